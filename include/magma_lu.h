@@ -1,0 +1,224 @@
+/*
+ * magma_lu.h -- C ABI of the GB300-native batched LU factor-and-solve library
+ * (libmagma_lu.so).
+ *
+ * The names, argument order, argument meaning, return codes and pivot/info
+ * conventions are those of MAGMA 2.x, so that code written against MAGMA's
+ * batched LU entry points links against this library unchanged.  Every
+ * declaration below cites the MAGMA interface it replaces, by the path of the
+ * file inside the MAGMA source tree.  MAGMA writes its batched routines once
+ * in double-complex ("z") and generates the d/s files at build time; the
+ * citations point to the z templates (read z -> d, magmaDoubleComplex ->
+ * double).
+ *
+ * Conventions (identical to MAGMA):
+ *   - magma_int_t is a 32-bit int (LP64 build; include/magma_types.h:68-71).
+ *   - Matrices are column-major, element (i,j) of matrix k at
+ *     dA_array[k][i + j*ldda].
+ *   - All arrays passed to batched routines -- the pointer arrays themselves,
+ *     the matrices, the pivot vectors and the info vector -- live in device
+ *     memory and are owned by the caller.
+ *   - Pivots are 1-based, LAPACK sequential-interchange order: row i of the
+ *     matrix was interchanged with row ipiv[i].
+ *   - info[k] = 0 on success, or j > 0 when U(j,j) of matrix k is exactly
+ *     zero (the factorisation still completes).
+ *   - A negative return value -i means argument i was illegal; the routine
+ *     then prints a message through magma_xerbla and does nothing else.
+ *   - Every routine only enqueues work on the queue's CUDA stream; none
+ *     synchronises the host unless its description says so.
+ */
+#ifndef MAGMA_LU_H
+#define MAGMA_LU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Types and constants -- include/magma_types.h:68-100, 549-634            */
+
+typedef int magma_int_t;              /* include/magma_types.h:71 (LP64) */
+typedef int magma_device_t;           /* include/magma_types.h:101 */
+typedef void *magma_ptr;
+typedef struct magma_queue *magma_queue_t;   /* include/magma_types.h:99-100 */
+
+#define MAGMA_SUCCESS               0
+#define MAGMA_ERR                  -100
+#define MAGMA_ERR_NOT_INITIALIZED  -101
+#define MAGMA_ERR_NOT_SUPPORTED    -103
+#define MAGMA_ERR_HOST_ALLOC       -112
+#define MAGMA_ERR_DEVICE_ALLOC     -113
+#define MAGMA_ERR_INVALID_PTR      -115
+#define MAGMA_ERR_UNKNOWN          -116
+#define MAGMA_ERR_NOT_IMPLEMENTED  -117
+
+typedef enum {
+    MagmaNoTrans   = 111,
+    MagmaTrans     = 112,
+    MagmaConjTrans = 113
+} magma_trans_t;                      /* include/magma_types.h:613-618 */
+
+/* ------------------------------------------------------------------------ */
+/* Runtime subset -- include/magma_auxiliary.h:24-25, 82-105, 258-330, 357 */
+
+magma_int_t magma_init(void);         /* interface_cuda/interface.cpp:164 */
+magma_int_t magma_finalize(void);     /* interface_cuda/interface.cpp:237 */
+
+/* Prints "Error in <name>, function-specific error (info = <info>)" to
+ * stderr, like control/xerbla.cpp:51. */
+void magma_xerbla(const char *name, magma_int_t info);
+
+/* MAGMA's magma_queue_create(device, &queue) macro expands to this call
+ * (include/magma_auxiliary.h:258-260).  The queue owns a new non-blocking
+ * CUDA stream. */
+void magma_queue_create_internal(magma_device_t device, magma_queue_t *queue_ptr,
+                                 const char *func, const char *file, int line);
+
+/* include/magma_auxiliary.h:284-292.  Wraps an existing cudaStream_t (passed
+ * as void* so that this header needs no CUDA include).  The cuBLAS and
+ * cuSPARSE handles are accepted for ABI compatibility and ignored: no routine
+ * here calls either library. */
+void magma_queue_create_from_cuda_internal(magma_device_t device, void *cuda_stream,
+                                           void *cublas_handle, void *cusparse_handle,
+                                           magma_queue_t *queue_ptr,
+                                           const char *func, const char *file, int line);
+
+void magma_queue_destroy_internal(magma_queue_t queue,
+                                  const char *func, const char *file, int line);
+void magma_queue_sync_internal(magma_queue_t queue,
+                               const char *func, const char *file, int line);
+magma_int_t magma_queue_get_device(magma_queue_t queue);
+/* Returns the queue's cudaStream_t (as void*). */
+void *magma_queue_get_cuda_stream(magma_queue_t queue);
+
+#define magma_queue_create(device, queue_ptr) \
+    magma_queue_create_internal(device, queue_ptr, __func__, __FILE__, __LINE__)
+#define magma_queue_create_from_cuda(device, stream, cublas, cusparse, queue_ptr) \
+    magma_queue_create_from_cuda_internal(device, stream, cublas, cusparse, queue_ptr, \
+                                          __func__, __FILE__, __LINE__)
+#define magma_queue_destroy(queue) \
+    magma_queue_destroy_internal(queue, __func__, __FILE__, __LINE__)
+#define magma_queue_sync(queue) \
+    magma_queue_sync_internal(queue, __func__, __FILE__, __LINE__)
+
+/* Device and pinned-host memory (include/magma_auxiliary.h:82-105). */
+magma_int_t magma_malloc(magma_ptr *ptr_ptr, size_t bytes);
+magma_int_t magma_malloc_pinned(void **ptr_ptr, size_t bytes);
+magma_int_t magma_free_internal(magma_ptr ptr, const char *func, const char *file, int line);
+magma_int_t magma_free_pinned_internal(void *ptr, const char *func, const char *file, int line);
+#define magma_free(ptr)        magma_free_internal(ptr, __func__, __FILE__, __LINE__)
+#define magma_free_pinned(ptr) magma_free_pinned_internal(ptr, __func__, __FILE__, __LINE__)
+
+/* Host <-> device vector copies, asynchronous on the queue's stream followed
+ * by a stream synchronisation, like include/magma_copy.h:27-30. */
+void magma_setvector_internal(magma_int_t n, magma_int_t elemSize,
+                              const void *hx_src, magma_int_t incx,
+                              magma_ptr dy_dst, magma_int_t incy, magma_queue_t queue,
+                              const char *func, const char *file, int line);
+void magma_getvector_internal(magma_int_t n, magma_int_t elemSize,
+                              const void *dx_src, magma_int_t incx,
+                              void *hy_dst, magma_int_t incy, magma_queue_t queue,
+                              const char *func, const char *file, int line);
+#define magma_setvector(n, elemSize, hx, incx, dy, incy, queue) \
+    magma_setvector_internal(n, elemSize, hx, incx, dy, incy, queue, __func__, __FILE__, __LINE__)
+#define magma_getvector(n, elemSize, dx, incx, hy, incy, queue) \
+    magma_getvector_internal(n, elemSize, dx, incx, hy, incy, queue, __func__, __FILE__, __LINE__)
+
+/* Pointer-array helpers: output_array[k] = input + k*batch_offset + row +
+ * column*lda (magmablas/zset_pointer.cu:20-25, include/magma_zbatched.h:28,
+ * include/magma_batched.h:63). */
+void magma_dset_pointer(double **output_array, double *input, magma_int_t lda,
+                        magma_int_t row, magma_int_t column, magma_int_t batch_offset,
+                        magma_int_t batchCount, magma_queue_t queue);
+void magma_sset_pointer(float **output_array, float *input, magma_int_t lda,
+                        magma_int_t row, magma_int_t column, magma_int_t batch_offset,
+                        magma_int_t batchCount, magma_queue_t queue);
+void magma_iset_pointer(magma_int_t **output_array, magma_int_t *input, magma_int_t lda,
+                        magma_int_t row, magma_int_t column, magma_int_t batch_offset,
+                        magma_int_t batchCount, magma_queue_t queue);
+
+/* ------------------------------------------------------------------------ */
+/* Batched LU, fixed size -- include/magma_zbatched.h                       */
+
+/* A = P*L*U for batchCount m-by-n matrices (include/magma_zbatched.h:848,
+ * src/zgetrf_batched.cpp:82-213).  Returns 0 or -1 (m<0), -2 (n<0),
+ * -4 (ldda<max(1,m)).  Workspace comes from the queue; the call neither
+ * allocates per call nor synchronises the host. */
+magma_int_t magma_dgetrf_batched(magma_int_t m, magma_int_t n,
+                                 double **dA_array, magma_int_t ldda,
+                                 magma_int_t **ipiv_array, magma_int_t *info_array,
+                                 magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetrf_batched(magma_int_t m, magma_int_t n,
+                                 float **dA_array, magma_int_t ldda,
+                                 magma_int_t **ipiv_array, magma_int_t *info_array,
+                                 magma_int_t batchCount, magma_queue_t queue);
+
+/* Square n <= 32 factorisation in registers (include/magma_zbatched.h:865,
+ * magmablas/zgetrf_batched_smallsq_noshfl.cu:193-285).  Returns -100 when
+ * n > 32. */
+magma_int_t magma_dgetrf_batched_smallsq_noshfl(magma_int_t n,
+                                                double **dA_array, magma_int_t ldda,
+                                                magma_int_t **ipiv_array, magma_int_t *info_array,
+                                                magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetrf_batched_smallsq_noshfl(magma_int_t n,
+                                                float **dA_array, magma_int_t ldda,
+                                                magma_int_t **ipiv_array, magma_int_t *info_array,
+                                                magma_int_t batchCount, magma_queue_t queue);
+
+/* Solve op(A)*X = B with the factors of magma_?getrf_batched
+ * (include/magma_zbatched.h:464, src/zgetrs_batched.cpp:86-181).
+ * trans is MagmaNoTrans, MagmaTrans or MagmaConjTrans (= MagmaTrans for real
+ * data).  Returns 0 or -1 (trans), -2 (n<0), -3 (nrhs<0), -5 (ldda<max(1,n)),
+ * -8 (lddb<max(1,n)). */
+magma_int_t magma_dgetrs_batched(magma_trans_t trans, magma_int_t n, magma_int_t nrhs,
+                                 double **dA_array, magma_int_t ldda,
+                                 magma_int_t **dipiv_array,
+                                 double **dB_array, magma_int_t lddb,
+                                 magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetrs_batched(magma_trans_t trans, magma_int_t n, magma_int_t nrhs,
+                                 float **dA_array, magma_int_t ldda,
+                                 magma_int_t **dipiv_array,
+                                 float **dB_array, magma_int_t lddb,
+                                 magma_int_t batchCount, magma_queue_t queue);
+
+/* Factor and solve A*X = B (include/magma_zbatched.h:1009,
+ * src/zgesv_batched.cpp:93-154).  Returns 0 or -1 (n<0), -2 (nrhs<0),
+ * -4 (ldda<max(1,n)), -6 (lddb<max(1,n)).  As in MAGMA, the solve runs even
+ * for matrices whose info is positive. */
+magma_int_t magma_dgesv_batched(magma_int_t n, magma_int_t nrhs,
+                                double **dA_array, magma_int_t ldda,
+                                magma_int_t **dipiv_array,
+                                double **dB_array, magma_int_t lddb,
+                                magma_int_t *dinfo_array,
+                                magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgesv_batched(magma_int_t n, magma_int_t nrhs,
+                                float **dA_array, magma_int_t ldda,
+                                magma_int_t **dipiv_array,
+                                float **dB_array, magma_int_t lddb,
+                                magma_int_t *dinfo_array,
+                                magma_int_t batchCount, magma_queue_t queue);
+
+/* Fused factor + solve for n <= 32 in one kernel (include/magma_zbatched.h:713,
+ * magmablas/zgesv_batched_small.cu:376-493).  MAGMA's version handles
+ * nrhs == 1 only; this one handles 1 <= nrhs <= 16.  Returns -100 (not
+ * applicable) for n > 32 or nrhs > 16, like MAGMA. */
+magma_int_t magma_dgesv_batched_small(magma_int_t n, magma_int_t nrhs,
+                                      double **dA_array, magma_int_t ldda,
+                                      magma_int_t **dipiv_array,
+                                      double **dB_array, magma_int_t lddb,
+                                      magma_int_t *dinfo_array,
+                                      magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgesv_batched_small(magma_int_t n, magma_int_t nrhs,
+                                      float **dA_array, magma_int_t ldda,
+                                      magma_int_t **dipiv_array,
+                                      float **dB_array, magma_int_t lddb,
+                                      magma_int_t *dinfo_array,
+                                      magma_int_t batchCount, magma_queue_t queue);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAGMA_LU_H */

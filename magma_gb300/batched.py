@@ -1,0 +1,161 @@
+"""Tensor-level wrappers over the MAGMA batched LU C ABI.
+
+Storage convention: a batch of column-major matrices is a CUDA tensor `S` of
+shape (batch, ncols, ld) whose element S[k, j, i] is A_k(i, j) -- exactly the
+memory MAGMA's dA_array[k][i + j*ldda] addresses.  `colmajor()` converts a
+(batch, m, n) math-oriented tensor to that storage and `from_colmajor()` back.
+
+Every routine enqueues on the current torch CUDA stream through a
+magma_queue_t wrapping it, returns without synchronising, and raises
+RuntimeError on a negative MAGMA return code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import torch
+
+from . import lib as _L
+
+_qlock = threading.Lock()
+_queues: dict[tuple[int, int], "Queue"] = {}
+
+
+class Queue:
+    """magma_queue_t around an existing CUDA stream (magma_queue_create_from_cuda)."""
+
+    def __init__(self, device: int, stream_handle: int):
+        lib = _L.load()
+        self._lib = lib
+        h = C.c_void_p()
+        lib.magma_queue_create_from_cuda_internal(device, C.c_void_p(stream_handle), None, None,
+                                                  C.byref(h), b"Queue", b"batched.py", 0)
+        if not h.value:
+            raise RuntimeError("magma_queue_create_from_cuda failed")
+        self.handle = h
+        self.device = device
+        self.stream_handle = stream_handle
+
+    def sync(self):
+        self._lib.magma_queue_sync_internal(self.handle, b"sync", b"batched.py", 0)
+
+    def __del__(self):
+        try:
+            self._lib.magma_queue_destroy_internal(self.handle, b"del", b"batched.py", 0)
+        except Exception:
+            pass
+
+    @staticmethod
+    def current(device: torch.device | int | None = None) -> "Queue":
+        if isinstance(device, int):
+            dev = device
+        elif device is not None and device.index is not None:
+            dev = device.index
+        else:
+            dev = torch.cuda.current_device()
+        s = torch.cuda.current_stream(dev).cuda_stream
+        key = (dev, s)
+        with _qlock:
+            q = _queues.get(key)
+            if q is None:
+                q = Queue(dev, s)
+                _queues[key] = q
+            return q
+
+
+def colmajor(A: torch.Tensor, ld: int | None = None) -> torch.Tensor:
+    """(batch, m, n) -> column-major storage (batch, n, ld), ld >= m."""
+    b, m, n = A.shape
+    ld = m if ld is None else ld
+    S = torch.zeros((b, n, ld), dtype=A.dtype, device=A.device)
+    S[:, :, :m] = A.transpose(1, 2)
+    return S
+
+
+def from_colmajor(S: torch.Tensor, m: int) -> torch.Tensor:
+    return S[:, :, :m].transpose(1, 2)
+
+
+def ptr_array(S: torch.Tensor) -> torch.Tensor:
+    """int64 device tensor holding the address of S[k] for every k (a T** array)."""
+    step = S.stride(0) * S.element_size()
+    return S.data_ptr() + torch.arange(S.shape[0], device=S.device, dtype=torch.int64) * step
+
+
+def _prefix(t: torch.Tensor) -> str:
+    if t.dtype == torch.float64:
+        return "d"
+    if t.dtype == torch.float32:
+        return "s"
+    raise TypeError(f"unsupported dtype {t.dtype}")
+
+
+def _check(rc: int, name: str):
+    if rc != 0:
+        raise RuntimeError(f"{name} returned {rc}")
+
+
+def _vp(t: torch.Tensor) -> C.c_void_p:
+    return C.c_void_p(t.data_ptr())
+
+
+def _check_storage(S: torch.Tensor, name: str):
+    if not S.is_cuda or S.dim() != 3 or S.stride(2) != 1 or S.stride(1) != S.shape[2]:
+        raise ValueError(f"{name} must be CUDA column-major storage (batch, ncols, ld), contiguous")
+
+
+def getrf_batched(S: torch.Tensor, m: int | None = None, ipiv: torch.Tensor | None = None,
+                  info: torch.Tensor | None = None, queue: Queue | None = None):
+    """In-place LU of every matrix in S (magma_?getrf_batched). Returns (ipiv, info)."""
+    _check_storage(S, "S")
+    b, n, ld = S.shape
+    m = ld if m is None else m
+    mn = min(m, n)
+    ipiv = torch.empty((b, max(mn, 1)), dtype=torch.int32, device=S.device) if ipiv is None else ipiv
+    info = torch.empty((b,), dtype=torch.int32, device=S.device) if info is None else info
+    q = queue or Queue.current(S.device)
+    lib = _L.load()
+    p = _prefix(S)
+    dA = ptr_array(S)
+    dP = ptr_array(ipiv)
+    rc = getattr(lib, f"magma_{p}getrf_batched")(m, n, _vp(dA), ld, _vp(dP), _vp(info), b, q.handle)
+    _check(rc, f"magma_{p}getrf_batched")
+    return ipiv, info
+
+
+def getrs_batched(LU: torch.Tensor, ipiv: torch.Tensor, B: torch.Tensor, trans: bool = False,
+                  queue: Queue | None = None):
+    """Solve op(A) X = B in place in B (magma_?getrs_batched)."""
+    _check_storage(LU, "LU")
+    _check_storage(B, "B")
+    b, n, ld = LU.shape
+    nrhs, ldb = B.shape[1], B.shape[2]
+    q = queue or Queue.current(LU.device)
+    lib = _L.load()
+    p = _prefix(LU)
+    tr = _L.MagmaTrans if trans else _L.MagmaNoTrans
+    rc = getattr(lib, f"magma_{p}getrs_batched")(
+        tr, n, nrhs, _vp(ptr_array(LU)), ld, _vp(ptr_array(ipiv)),
+        _vp(ptr_array(B)), ldb, b, q.handle)
+    _check(rc, f"magma_{p}getrs_batched")
+    return B
+
+
+def gesv_batched(S: torch.Tensor, B: torch.Tensor, ipiv: torch.Tensor | None = None,
+                 info: torch.Tensor | None = None, queue: Queue | None = None):
+    """Factor S and solve in place (magma_?gesv_batched). Returns (ipiv, info)."""
+    _check_storage(S, "S")
+    _check_storage(B, "B")
+    b, n, ld = S.shape
+    nrhs, ldb = B.shape[1], B.shape[2]
+    ipiv = torch.empty((b, max(n, 1)), dtype=torch.int32, device=S.device) if ipiv is None else ipiv
+    info = torch.empty((b,), dtype=torch.int32, device=S.device) if info is None else info
+    q = queue or Queue.current(S.device)
+    lib = _L.load()
+    p = _prefix(S)
+    rc = getattr(lib, f"magma_{p}gesv_batched")(
+        n, nrhs, _vp(ptr_array(S)), ld, _vp(ptr_array(ipiv)), _vp(ptr_array(B)),
+        ldb, _vp(info), b, q.handle)
+    _check(rc, f"magma_{p}gesv_batched")
+    return ipiv, info

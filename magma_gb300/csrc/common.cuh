@@ -1,0 +1,107 @@
+// common.cuh -- shared definitions for the GB300 batched LU kernels.
+//
+// Arithmetic contract shared by every kernel in this library: each update of
+// a matrix or right-hand-side element is one fused multiply-add
+// a = fma(-l, u, a), applied in increasing elimination order with a single
+// accumulator per element, the column below a pivot is scaled by the
+// reciprocal of the pivot (or divided by it when |pivot| < sfmin, as LAPACK
+// dgetf2 does), and the U solve multiplies by the same reciprocal.  Any
+// schedule that honours this contract returns bit-identical factors, pivots
+// and solutions, which is what the parity tests check.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include "../../include/magma_lu.h"
+
+struct magma_queue {
+    int device;
+    cudaStream_t stream;
+    bool own_stream;
+    // Queue-owned device workspace, grown on demand by routines that need
+    // scratch space (never by the factor/solve routines themselves).
+    void *work;
+    size_t work_bytes;
+};
+
+namespace mlu {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Precision traits.
+template <typename T> struct Prec;
+template <> struct Prec<double> {
+    // bit pattern helpers: exponent field non-zero <=> |x| >= DBL_MIN or x is
+    // inf/NaN, i.e. the reciprocal of x does not overflow.
+    __device__ static inline bool normal_or_special(double x) {
+        return (__double2hiint(x) & 0x7ff00000) != 0;
+    }
+    __device__ static inline bool nonzero(double x) {
+        return ((__double_as_longlong(x) << 1) != 0);
+    }
+    __device__ static inline bool isnan_(double x) {
+        return (((unsigned long long)__double_as_longlong(x)) << 1) > (0x7ff0000000000000ull << 1);
+    }
+    // |x| as a 63-bit unsigned key (monotone in |x| for non-NaN x).
+    __device__ static inline unsigned long long absbits(double x) {
+        return ((unsigned long long)__double_as_longlong(x)) & 0x7fffffffffffffffull;
+    }
+    __device__ static inline double fma_(double a, double b, double c) { return fma(a, b, c); }
+};
+template <> struct Prec<float> {
+    __device__ static inline bool normal_or_special(float x) {
+        return (__float_as_uint(x) & 0x7f800000u) != 0;
+    }
+    __device__ static inline bool nonzero(float x) { return (__float_as_uint(x) << 1) != 0; }
+    __device__ static inline bool isnan_(float x) {
+        return (__float_as_uint(x) << 1) > (0x7f800000u << 1);
+    }
+    __device__ static inline unsigned long long absbits(float x) {
+        return (unsigned long long)(__float_as_uint(x) & 0x7fffffffu);
+    }
+    __device__ static inline float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+};
+
+// x scaled by the reciprocal r of d, or divided by d when d is subnormal
+// (LAPACK dgetf2's sfmin rule).
+template <typename T>
+__device__ __forceinline__ T rscale(T x, T d, T r) {
+    return Prec<T>::normal_or_special(d) ? x * r : x / d;
+}
+
+// ---------------------------------------------------------------------------
+// Warp arg-max of a 64-bit key with ties resolved to the smallest `pos`.
+// Returns the winning pos (all lanes agree).  Uses redux.sync on 32-bit
+// halves so that the search never touches the floating-point pipes.
+__device__ __forceinline__ unsigned warp_argmax_key(unsigned long long key, unsigned pos) {
+    unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+    unsigned mhi = __reduce_max_sync(FULL, hi);
+    unsigned mlo = __reduce_max_sync(FULL, hi == mhi ? lo : 0u);
+    bool cand = (hi == mhi) && (lo == mlo);
+    return __reduce_min_sync(FULL, cand ? pos : 0xffffffffu);
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl(T v, int src) { return __shfl_sync(FULL, v, src); }
+
+}  // namespace mlu
+
+#define MLU_CHECK_LAUNCH()                                                              \
+    do {                                                                                \
+        cudaError_t e_ = cudaGetLastError();                                            \
+        if (e_ != cudaSuccess) {                                                        \
+            fprintf(stderr, "magma_lu: launch failed in %s: %s\n", __func__,            \
+                    cudaGetErrorString(e_));                                            \
+            return MAGMA_ERR_UNKNOWN;                                                   \
+        }                                                                               \
+    } while (0)
+
+static inline magma_int_t mlu_max(magma_int_t a, magma_int_t b) { return a > b ? a : b; }
+static inline magma_int_t mlu_min(magma_int_t a, magma_int_t b) { return a < b ? a : b; }
+static inline magma_int_t mlu_ceildiv(magma_int_t a, magma_int_t b) { return (a + b - 1) / b; }
+
+// Batches are launched in chunks of at most this many matrices per grid
+// dimension (gridDim.y/z limit), like MAGMA's max_batchCount.
+constexpr magma_int_t MLU_MAX_GRID_Y = 65535;

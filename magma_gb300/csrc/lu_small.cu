@@ -1,0 +1,315 @@
+// lu_small.cu -- warp-per-matrix LU factor / solve for n <= 32.
+//
+// Replaces, for one warp per matrix instead of one CTA per matrix:
+//   magma_dgesv_batched_small           magmablas/zgesv_batched_small.cu:49-162,376-493
+//   magma_dgetrf_batched_smallsq_noshfl magmablas/zgetrf_batched_smallsq_noshfl.cu:40-285
+//   the n <= 32 part of magma_dgetrs_batched  src/zgetrs_batched.cpp:86-181
+//
+// Layout: lane i of the warp holds row i of the matrix (n values in
+// registers) and row i of the right-hand sides.  Rows never move during the
+// elimination ("lazy" interchange, as the reference kernels do); each lane
+// tracks the row's position in LAPACK's current row order, which is what the
+// pivot search breaks ties on and where the row is written at the end.
+//
+// Pivot search runs on the integer pipes: |a| as an unsigned 63-bit key,
+// reduced with redux.sync on the two 32-bit halves, ties to the smallest
+// current position.  NaN follows idamax's strict '>' scan: a NaN at the
+// current diagonal position wins, any other NaN never does.
+//
+// GB300 note: FP64 issues at a small fraction of the FP32 rate on this part,
+// so the kernel keeps everything except the eliminations themselves (pivot
+// search, interchanges, broadcasts) off the FP64 pipe, and the U solve reuses
+// the pivot reciprocals computed during the factorisation.
+#include "common.cuh"
+
+namespace mlu {
+
+constexpr int SMALL_WARPS = 4;   // matrices per CTA
+
+template <typename T, int N, int NRHS>
+__global__ void __launch_bounds__(SMALL_WARPS * 32)
+small_gesv_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T **dB_array,
+                  int lddb, int *info_array, int batch)
+{
+    const int lane = threadIdx.x & 31;
+    const int mat = blockIdx.x * SMALL_WARPS + (threadIdx.x >> 5);
+    if (mat >= batch) return;   // uniform per warp
+
+    T *A = dA_array[mat];
+    const bool row_valid = lane < n;
+
+    T a[N];
+#pragma unroll
+    for (int j = 0; j < N; j++)
+        a[j] = (row_valid && j < n) ? A[lane + (size_t)j * ldda] : T(0);
+
+    constexpr int NB = NRHS > 0 ? NRHS : 1;
+    T b[NB];
+    T *B = nullptr;
+    if (NRHS > 0) {
+        B = dB_array[mat];
+#pragma unroll
+        for (int c = 0; c < NB; c++)
+            b[c] = (row_valid && c < nrhs) ? B[lane + (size_t)c * lddb] : T(0);
+    }
+
+    unsigned pos = lane;      // position in LAPACK's current row order
+    bool active = row_valid;  // not yet chosen as a pivot row
+    int info = 0;
+    int my_ipiv = 0;
+    T my_rcp = T(0);          // reciprocal of this row's pivot, once it is one
+
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        if (k >= n) break;
+        const T v = a[k];
+        unsigned long long key = 0ull;
+        if (active) {
+            unsigned long long mag = Prec<T>::absbits(v);
+            if (Prec<T>::isnan_(v)) mag = (pos == (unsigned)k) ? 0x7fffffffffffffffull : 0ull;
+            key = mag | 0x8000000000000000ull;
+        }
+        const unsigned ppos = warp_argmax_key(key, active ? pos : 0xffffffffu);
+        const int plane = __ffs(__ballot_sync(FULL, active && pos == ppos)) - 1;
+        const T piv = shfl(v, plane);
+        const bool nz = Prec<T>::nonzero(piv);
+        if (!nz && info == 0) info = k + 1;
+        const T r = T(1) / piv;
+        if (lane == k) my_ipiv = (int)ppos + 1;
+        const bool was_k = (pos == (unsigned)k);
+        if (lane == plane) { pos = k; active = false; my_rcp = r; }
+        else if (was_k) pos = ppos;
+
+        const T l = (active && nz) ? rscale(v, piv, r) : v;
+        if (active) a[k] = l;
+#pragma unroll
+        for (int j = k + 1; j < N; j++) {
+            if (j < n) {
+                const T u = shfl(a[j], plane);
+                if (active) a[j] = Prec<T>::fma_(-l, u, a[j]);
+            }
+        }
+        if (NRHS > 0) {
+#pragma unroll
+            for (int c = 0; c < NB; c++) {
+                if (c < nrhs) {
+                    const T u = shfl(b[c], plane);
+                    if (active) b[c] = Prec<T>::fma_(-l, u, b[c]);
+                }
+            }
+        }
+    }
+
+    if (NRHS > 0) {
+        // U x = y, column-oriented, multiplying by the stored pivot reciprocals.
+#pragma unroll
+        for (int t = N - 1; t >= 0; t--) {
+            if (t >= n) continue;
+            const int tl = __ffs(__ballot_sync(FULL, row_valid && pos == (unsigned)t)) - 1;
+            const T d = shfl(a[t], tl);
+            const T rr = shfl(my_rcp, tl);
+#pragma unroll
+            for (int c = 0; c < NB; c++) {
+                if (c < nrhs) {
+                    const T x = rscale(shfl(b[c], tl), d, rr);
+                    if (lane == tl) b[c] = x;
+                    else if (row_valid && pos < (unsigned)t) b[c] = Prec<T>::fma_(-a[t], x, b[c]);
+                }
+            }
+        }
+    }
+
+    if (row_valid) {
+#pragma unroll
+        for (int j = 0; j < N; j++)
+            if (j < n) A[pos + (size_t)j * ldda] = a[j];
+        ipiv_array[mat][lane] = my_ipiv;
+        if (NRHS > 0) {
+#pragma unroll
+            for (int c = 0; c < NB; c++)
+                if (c < nrhs) B[pos + (size_t)c * lddb] = b[c];
+        }
+    }
+    if (lane == 0) info_array[mat] = info;
+}
+
+// Solve with existing factors, n <= 32.  NoTrans: lane i holds row i of LU.
+// Trans: lane i holds column i of LU, so that U(t,i) and L(t,i) are static
+// register indices.  RHS columns [blockIdx.y*NRHS, +NRHS).
+template <typename T, int N, int NRHS, bool TRANS>
+__global__ void __launch_bounds__(SMALL_WARPS * 32)
+small_getrs_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T **dB_array,
+                   int lddb, int batch)
+{
+    const int lane = threadIdx.x & 31;
+    const int mat = blockIdx.x * SMALL_WARPS + (threadIdx.x >> 5);
+    if (mat >= batch) return;
+    const int c0 = blockIdx.y * NRHS;
+    const T *A = dA_array[mat];
+    const int *ipiv = ipiv_array[mat];
+    T *B = dB_array[mat] + (size_t)c0 * lddb;
+    const int nr = min(NRHS, nrhs - c0);
+    const bool valid = lane < n;
+
+    T a[N];
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+        if (TRANS) a[j] = (valid && j < n) ? A[j + (size_t)lane * ldda] : T(0);
+        else       a[j] = (valid && j < n) ? A[lane + (size_t)j * ldda] : T(0);
+    }
+    T b[NRHS];
+#pragma unroll
+    for (int c = 0; c < NRHS; c++) b[c] = (valid && c < nr) ? B[lane + (size_t)c * lddb] : T(0);
+    const int my_piv = valid ? ipiv[lane] - 1 : lane;
+
+    if (!TRANS) {
+        // B <- P B, sequential interchanges k = 0..n-1
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            if (k >= n) break;
+            const int p = shfl(my_piv, k);
+            if (p != k) {
+#pragma unroll
+                for (int c = 0; c < NRHS; c++) {
+                    const T vk = shfl(b[c], k), vp = shfl(b[c], p);
+                    if (lane == k) b[c] = vp;
+                    if (lane == p) b[c] = vk;
+                }
+            }
+        }
+        // L y = b (unit lower)
+#pragma unroll
+        for (int t = 0; t < N; t++) {
+            if (t >= n) break;
+#pragma unroll
+            for (int c = 0; c < NRHS; c++) {
+                const T y = shfl(b[c], t);
+                if (lane > t) b[c] = Prec<T>::fma_(-a[t], y, b[c]);
+            }
+        }
+        // U x = y
+#pragma unroll
+        for (int t = N - 1; t >= 0; t--) {
+            if (t >= n) continue;
+            const T d = shfl(a[t], t);
+            const T r = T(1) / d;
+#pragma unroll
+            for (int c = 0; c < NRHS; c++) {
+                const T x = rscale(shfl(b[c], t), d, r);
+                if (lane == t) b[c] = x;
+                else if (lane < t) b[c] = Prec<T>::fma_(-a[t], x, b[c]);
+            }
+        }
+    } else {
+        // U^T y = b: lane i holds column i, so a[t] = U(t,i) for t <= i.
+#pragma unroll
+        for (int t = 0; t < N; t++) {
+            if (t >= n) break;
+            const T d = shfl(a[t], t);
+            const T r = T(1) / d;
+#pragma unroll
+            for (int c = 0; c < NRHS; c++) {
+                const T x = rscale(shfl(b[c], t), d, r);
+                if (lane == t) b[c] = x;
+                else if (lane > t) b[c] = Prec<T>::fma_(-a[t], x, b[c]);
+            }
+        }
+        // L^T x = y: a[t] = L(t,i) for t > i.
+#pragma unroll
+        for (int t = N - 1; t >= 0; t--) {
+            if (t >= n) continue;
+#pragma unroll
+            for (int c = 0; c < NRHS; c++) {
+                const T x = shfl(b[c], t);
+                if (lane < t) b[c] = Prec<T>::fma_(-a[t], x, b[c]);
+            }
+        }
+        // B <- P^T B, interchanges in reverse order
+#pragma unroll
+        for (int k = N - 1; k >= 0; k--) {
+            if (k >= n) continue;
+            const int p = shfl(my_piv, k);
+            if (p != k) {
+#pragma unroll
+                for (int c = 0; c < NRHS; c++) {
+                    const T vk = shfl(b[c], k), vp = shfl(b[c], p);
+                    if (lane == k) b[c] = vp;
+                    if (lane == p) b[c] = vk;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NRHS; c++)
+        if (valid && c < nr) B[lane + (size_t)c * lddb] = b[c];
+}
+
+template <typename T, int N, int NRHS>
+static void launch_small_gesv(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb,
+                              int *info, int batch, cudaStream_t s)
+{
+    small_gesv_kernel<T, N, NRHS><<<mlu_ceildiv(batch, SMALL_WARPS), SMALL_WARPS * 32, 0, s>>>(
+        n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch);
+}
+
+template <typename T, int N>
+static void dispatch_nrhs(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb,
+                          int *info, int batch, cudaStream_t s)
+{
+    if (nrhs == 0)      launch_small_gesv<T, N, 0>(n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch, s);
+    else if (nrhs == 1) launch_small_gesv<T, N, 1>(n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch, s);
+    else if (nrhs <= 4) launch_small_gesv<T, N, 4>(n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch, s);
+    else                launch_small_gesv<T, N, 16>(n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch, s);
+}
+
+// Fused factor (+ solve when nrhs > 0) for n <= 32, nrhs <= 16.
+template <typename T>
+magma_int_t small_gesv(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb, int *info,
+                       int batch, magma_queue_t q)
+{
+    if (n > 32 || n < 1 || nrhs > 16) return MAGMA_ERR;   // -100: not applicable
+    if (batch <= 0) return MAGMA_SUCCESS;
+    cudaStream_t s = q->stream;
+    if (n <= 8)       dispatch_nrhs<T, 8>(n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch, s);
+    else if (n <= 16) dispatch_nrhs<T, 16>(n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch, s);
+    else              dispatch_nrhs<T, 32>(n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch, s);
+    MLU_CHECK_LAUNCH();
+    return MAGMA_SUCCESS;
+}
+
+template <typename T, int N, bool TRANS>
+static void launch_small_getrs(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb,
+                               int batch, cudaStream_t s)
+{
+    constexpr int NR = 4;
+    dim3 grid(mlu_ceildiv(batch, SMALL_WARPS), mlu_ceildiv(nrhs, NR));
+    small_getrs_kernel<T, N, NR, TRANS><<<grid, SMALL_WARPS * 32, 0, s>>>(
+        n, nrhs, dA, ldda, ipiv, dB, lddb, batch);
+}
+
+template <typename T>
+magma_int_t small_getrs(bool trans, int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB,
+                        int lddb, int batch, magma_queue_t q)
+{
+    if (n > 32) return MAGMA_ERR;
+    if (batch <= 0 || n == 0 || nrhs == 0) return MAGMA_SUCCESS;
+    cudaStream_t s = q->stream;
+    if (trans) {
+        if (n <= 8)       launch_small_getrs<T, 8, true>(n, nrhs, dA, ldda, ipiv, dB, lddb, batch, s);
+        else if (n <= 16) launch_small_getrs<T, 16, true>(n, nrhs, dA, ldda, ipiv, dB, lddb, batch, s);
+        else              launch_small_getrs<T, 32, true>(n, nrhs, dA, ldda, ipiv, dB, lddb, batch, s);
+    } else {
+        if (n <= 8)       launch_small_getrs<T, 8, false>(n, nrhs, dA, ldda, ipiv, dB, lddb, batch, s);
+        else if (n <= 16) launch_small_getrs<T, 16, false>(n, nrhs, dA, ldda, ipiv, dB, lddb, batch, s);
+        else              launch_small_getrs<T, 32, false>(n, nrhs, dA, ldda, ipiv, dB, lddb, batch, s);
+    }
+    MLU_CHECK_LAUNCH();
+    return MAGMA_SUCCESS;
+}
+
+template magma_int_t small_gesv<double>(int, int, double **, int, int **, double **, int, int *, int, magma_queue_t);
+template magma_int_t small_gesv<float>(int, int, float **, int, int **, float **, int, int *, int, magma_queue_t);
+template magma_int_t small_getrs<double>(bool, int, int, double **, int, int **, double **, int, int, magma_queue_t);
+template magma_int_t small_getrs<float>(bool, int, int, float **, int, int **, float **, int, int, magma_queue_t);
+
+}  // namespace mlu

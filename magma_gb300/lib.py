@@ -1,0 +1,82 @@
+"""ctypes binding of libmagma_lu.so (the C ABI declared in include/magma_lu.h).
+
+Loading fails loudly: there is no CPU fallback for any routine of this
+package.  Function names and argument order are MAGMA's.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libmagma_lu.so"
+
+_lock = threading.Lock()
+_lib = None
+
+c_int = C.c_int
+c_ptr = C.c_void_p
+
+# argtypes of each exported routine (all pointers as void*)
+_PROTOS = {
+    "magma_init": ([], c_int),
+    "magma_finalize": ([], c_int),
+    "magma_xerbla": ([C.c_char_p, c_int], None),
+    "magma_queue_create_internal": ([c_int, c_ptr, C.c_char_p, C.c_char_p, c_int], None),
+    "magma_queue_create_from_cuda_internal": (
+        [c_int, c_ptr, c_ptr, c_ptr, c_ptr, C.c_char_p, C.c_char_p, c_int], None),
+    "magma_queue_destroy_internal": ([c_ptr, C.c_char_p, C.c_char_p, c_int], None),
+    "magma_queue_sync_internal": ([c_ptr, C.c_char_p, C.c_char_p, c_int], None),
+    "magma_queue_get_device": ([c_ptr], c_int),
+    "magma_queue_get_cuda_stream": ([c_ptr], c_ptr),
+    "magma_malloc": ([c_ptr, C.c_size_t], c_int),
+    "magma_malloc_pinned": ([c_ptr, C.c_size_t], c_int),
+    "magma_free_internal": ([c_ptr, C.c_char_p, C.c_char_p, c_int], c_int),
+    "magma_free_pinned_internal": ([c_ptr, C.c_char_p, C.c_char_p, c_int], c_int),
+    "magma_setvector_internal": (
+        [c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, C.c_char_p, C.c_char_p, c_int], None),
+    "magma_getvector_internal": (
+        [c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, C.c_char_p, C.c_char_p, c_int], None),
+    "magma_dset_pointer": ([c_ptr, c_ptr, c_int, c_int, c_int, c_int, c_int, c_ptr], None),
+    "magma_sset_pointer": ([c_ptr, c_ptr, c_int, c_int, c_int, c_int, c_int, c_ptr], None),
+    "magma_iset_pointer": ([c_ptr, c_ptr, c_int, c_int, c_int, c_int, c_int, c_ptr], None),
+}
+for _p in "ds":
+    _PROTOS[f"magma_{_p}getrf_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}getrf_batched_smallsq_noshfl"] = ([c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}getrs_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}gesv_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}gesv_batched_small"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr, c_int, c_ptr], c_int)
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load libmagma_lu.so (building it first if the CUDA toolkit is present)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = Path(path) if path else LIB_PATH
+        if path is None:
+            from . import build as _build
+            if not _build.up_to_date():
+                _build.build()
+        if not p.exists():
+            raise RuntimeError(f"{p} is missing: build it with magma_gb300.build.build()")
+        lib = C.CDLL(str(p))
+        for name, (args, res) in _PROTOS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+        return lib
+
+
+def exported_names() -> list[str]:
+    return sorted(_PROTOS)
+
+
+MagmaNoTrans = 111
+MagmaTrans = 112
+MagmaConjTrans = 113

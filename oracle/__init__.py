@@ -1,0 +1,11 @@
+"""CPU oracle for the batched LU path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+package, as the checker and as the timed CPU reference; the product path never
+imports it.  See lu_oracle.c for the algorithm and the reference lines it
+restates.  The restatement is pinned against LAPACK (the library the
+reference's CPU check path calls) by the golden fixtures in tests/golden/.
+"""
+from .oracle import (build, dgesv_batched, dgetrf, dgetrf_batched, dgetrs, dgetrs_batched,  # noqa: F401
+                     dgesv_vbatched, load, max_threads, sgesv_batched, sgetrf, sgetrf_batched,
+                     sgetrs, sgetrs_batched)

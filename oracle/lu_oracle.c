@@ -1,0 +1,200 @@
+/*
+ * lu_oracle.c -- CPU restatement of MAGMA's batched LU factor-and-solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: the tests, the smoke
+ * entry and the CPU-baseline leg of the benchmark call it to verify and to
+ * time against; no product code path links or calls it.
+ *
+ * Algorithm (right-looking, column by column, partial pivoting), restating:
+ *   - LAPACK dgetf2 as called by the reference's CPU check path
+ *     (testing/testing_zgesv_batched.cpp:160-176 calls lapackf77_?gesv per
+ *     matrix under OpenMP): pivot = first entry of maximum magnitude in the
+ *     current row order (idamax: strict '>' scan), whole-row interchange,
+ *     column scaled by the reciprocal of the pivot when |pivot| >= sfmin and
+ *     divided by it otherwise, rank-1 update of the trailing matrix;
+ *   - MAGMA's pivot and info conventions: magmablas/zgesv_batched_small.cu:60-93
+ *     (first-max scan with strict '>', zero pivot leaves the column unscaled,
+ *     info = first zero-pivot column, 1-based pivots at :156) and
+ *     magmablas/magma_templates.h:44-60 (ties go to the lower index);
+ *   - triangular solves with the inverted diagonal multiplied in, like
+ *     magmablas/trsm_template_device.cuh:53-55.
+ *
+ * Arithmetic contract.  Every update is one fused multiply-add
+ * a = fma(-l, u, a), applied to each element in increasing elimination
+ * order.  Any blocked or parallel schedule that keeps one accumulator per
+ * element and applies its updates in that order (the GPU kernels do) gives
+ * bit-identical factors, pivots and solutions.  Compile with
+ * -ffp-contract=off so that the compiler adds no other contraction.
+ *
+ * Solve order (getrs):
+ *   NoTrans: B <- P*B (sequential interchanges k = 0..n-1), then for
+ *            t = 0..n-1: b_i = fma(-L(i,t), b_t, b_i) for i > t, then for
+ *            t = n-1..0: b_t = b_t*rcp(U(t,t)) and b_i = fma(-U(i,t), b_t, b_i)
+ *            for i < t.
+ *   Trans:   for t = 0..n-1: b_t = b_t*rcp(U(t,t)), b_i = fma(-U(t,i), b_t, b_i)
+ *            for i > t; then for t = n-1..0: b_i = fma(-L(t,i), b_t, b_i) for
+ *            i < t; then interchanges in reverse order k = n-1..0 (LAPACK
+ *            dgetrs with TRANS='T').
+ *   rcp(u) = 1/u when |u| >= sfmin, otherwise the element is divided by u.
+ */
+#include <math.h>
+#include <float.h>
+#include <stdint.h>
+#include <string.h>
+#include <stdlib.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define DEFINE_LU(T, P, FMA, FABS, SFMIN)                                              \
+                                                                                       \
+/* Scale x by the reciprocal of d, or divide when d is below sfmin (LAPACK dgetf2). */ \
+static inline T P##_rscale(T x, T d, T r)                                              \
+{                                                                                      \
+    return (FABS(d) >= SFMIN) ? x * r : x / d;                                         \
+}                                                                                      \
+                                                                                       \
+/* First index of maximum |a| over a[0..len), strict '>' scan (idamax). */            \
+static int P##_iamax(int len, const T *a, int inc)                                     \
+{                                                                                      \
+    int best = 0;                                                                      \
+    T vmax = FABS(a[0]);                                                               \
+    for (int i = 1; i < len; i++) {                                                    \
+        T v = FABS(a[(size_t)i * inc]);                                                \
+        if (v > vmax) { vmax = v; best = i; }                                          \
+    }                                                                                  \
+    return best;                                                                       \
+}                                                                                      \
+                                                                                       \
+int oracle_##P##getrf(int m, int n, T *A, int lda, int *ipiv)                          \
+{                                                                                      \
+    int info = 0;                                                                      \
+    int mn = m < n ? m : n;                                                            \
+    for (int k = 0; k < mn; k++) {                                                     \
+        T *colk = A + (size_t)k * lda;                                                 \
+        int p = k + P##_iamax(m - k, colk + k, 1);                                     \
+        ipiv[k] = p + 1;                                                               \
+        if (colk[p] != (T)0) {                                                         \
+            if (p != k) {                                                              \
+                for (int j = 0; j < n; j++) {                                          \
+                    T *c = A + (size_t)j * lda;                                        \
+                    T t = c[k]; c[k] = c[p]; c[p] = t;                                 \
+                }                                                                      \
+            }                                                                          \
+            T piv = colk[k];                                                           \
+            T r = (T)1 / piv;                                                          \
+            for (int i = k + 1; i < m; i++) colk[i] = P##_rscale(colk[i], piv, r);     \
+        } else if (info == 0) {                                                        \
+            info = k + 1;                                                              \
+        }                                                                              \
+        for (int j = k + 1; j < n; j++) {                                              \
+            T *c = A + (size_t)j * lda;                                                \
+            T u = c[k];                                                                \
+            for (int i = k + 1; i < m; i++) c[i] = FMA(-colk[i], u, c[i]);             \
+        }                                                                              \
+    }                                                                                  \
+    return info;                                                                       \
+}                                                                                      \
+                                                                                       \
+void oracle_##P##getrs(int trans, int n, int nrhs, const T *LU, int lda,               \
+                       const int *ipiv, T *B, int ldb)                                 \
+{                                                                                      \
+    for (int c = 0; c < nrhs; c++) {                                                   \
+        T *b = B + (size_t)c * ldb;                                                    \
+        if (trans == 0) {                                                              \
+            for (int k = 0; k < n; k++) {                                              \
+                int p = ipiv[k] - 1;                                                   \
+                if (p != k) { T t = b[k]; b[k] = b[p]; b[p] = t; }                     \
+            }                                                                          \
+            for (int t = 0; t < n; t++) {                                              \
+                const T *l = LU + (size_t)t * lda;                                     \
+                for (int i = t + 1; i < n; i++) b[i] = FMA(-l[i], b[t], b[i]);         \
+            }                                                                          \
+            for (int t = n - 1; t >= 0; t--) {                                         \
+                const T *u = LU + (size_t)t * lda;                                     \
+                T d = u[t];                                                            \
+                b[t] = P##_rscale(b[t], d, (T)1 / d);                                  \
+                for (int i = 0; i < t; i++) b[i] = FMA(-u[i], b[t], b[i]);             \
+            }                                                                          \
+        } else {                                                                       \
+            for (int t = 0; t < n; t++) {                                              \
+                T d = LU[(size_t)t * lda + t];                                         \
+                b[t] = P##_rscale(b[t], d, (T)1 / d);                                  \
+                for (int i = t + 1; i < n; i++)                                        \
+                    b[i] = FMA(-LU[(size_t)i * lda + t], b[t], b[i]);                  \
+            }                                                                          \
+            for (int t = n - 1; t >= 0; t--) {                                         \
+                for (int i = 0; i < t; i++)                                            \
+                    b[i] = FMA(-LU[(size_t)i * lda + t], b[t], b[i]);                  \
+            }                                                                          \
+            for (int k = n - 1; k >= 0; k--) {                                         \
+                int p = ipiv[k] - 1;                                                   \
+                if (p != k) { T t = b[k]; b[k] = b[p]; b[p] = t; }                     \
+            }                                                                          \
+        }                                                                              \
+    }                                                                                  \
+}                                                                                      \
+                                                                                       \
+/* Strided batch: matrix k at A + k*strideA, etc.  OpenMP over the batch with  */     \
+/* dynamic scheduling, as testing/testing_zgesv_batched.cpp:160-176 does.      */     \
+void oracle_##P##getrf_batched(int m, int n, T *A, int lda, long strideA,             \
+                               int *ipiv, long strideP, int *info, int batch,         \
+                               int nthreads)                                          \
+{                                                                                      \
+    (void)nthreads;                                                                    \
+    _Pragma("omp parallel for schedule(dynamic) num_threads(nthreads)")               \
+    for (int k = 0; k < batch; k++)                                                    \
+        info[k] = oracle_##P##getrf(m, n, A + k * strideA, lda, ipiv + k * strideP);   \
+}                                                                                      \
+                                                                                       \
+void oracle_##P##getrs_batched(int trans, int n, int nrhs, const T *A, int lda,       \
+                               long strideA, const int *ipiv, long strideP,           \
+                               T *B, int ldb, long strideB, int batch, int nthreads)  \
+{                                                                                      \
+    (void)nthreads;                                                                    \
+    _Pragma("omp parallel for schedule(dynamic) num_threads(nthreads)")               \
+    for (int k = 0; k < batch; k++)                                                    \
+        oracle_##P##getrs(trans, n, nrhs, A + k * strideA, lda, ipiv + k * strideP,    \
+                          B + k * strideB, ldb);                                       \
+}                                                                                      \
+                                                                                       \
+void oracle_##P##gesv_batched(int n, int nrhs, T *A, int lda, long strideA,           \
+                              int *ipiv, long strideP, T *B, int ldb, long strideB,   \
+                              int *info, int batch, int nthreads)                     \
+{                                                                                      \
+    (void)nthreads;                                                                    \
+    _Pragma("omp parallel for schedule(dynamic) num_threads(nthreads)")               \
+    for (int k = 0; k < batch; k++) {                                                  \
+        info[k] = oracle_##P##getrf(n, n, A + k * strideA, lda, ipiv + k * strideP);   \
+        oracle_##P##getrs(0, n, nrhs, A + k * strideA, lda, ipiv + k * strideP,        \
+                          B + k * strideB, ldb);                                       \
+    }                                                                                  \
+}
+
+DEFINE_LU(double, d, fma, fabs, DBL_MIN)
+DEFINE_LU(float, s, fmaf, fabsf, FLT_MIN)
+
+/* Variable-size batch: matrix k is n[k]-by-n[k] at A + offA[k] with leading
+ * dimension lda[k]; nrhs[k] right-hand sides at B + offB[k] with ldb[k]. */
+void oracle_dgesv_vbatched(const int *n, const int *nrhs, double *A, const long *offA,
+                           const int *lda, int *ipiv, const long *offP, double *B,
+                           const long *offB, const int *ldb, int *info, int batch,
+                           int nthreads)
+{
+    (void)nthreads;
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+    for (int k = 0; k < batch; k++) {
+        info[k] = oracle_dgetrf(n[k], n[k], A + offA[k], lda[k], ipiv + offP[k]);
+        oracle_dgetrs(0, n[k], nrhs[k], A + offA[k], lda[k], ipiv + offP[k],
+                      B + offB[k], ldb[k]);
+    }
+}
+
+int oracle_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

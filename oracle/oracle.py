@@ -1,0 +1,181 @@
+"""ctypes wrapper of liblu_oracle.so (lu_oracle.c).  Test infrastructure only.
+
+Arrays follow LAPACK conventions: a batch of column-major matrices is a numpy
+array of shape (batch, ncols, ld) with element [k, j, i] = A_k(i, j), the same
+storage the GPU library uses.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "lu_oracle.c"
+LIB = HERE / "liblu_oracle.so"
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile lu_oracle.c with gcc (no FMA contraction, OpenMP over the batch)."""
+    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+           "-o", str(tmp), str(SRC), "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def load():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            _lib = C.CDLL(str(LIB))
+        return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def max_threads() -> int:
+    return int(load().oracle_max_threads())
+
+
+def _threads(nthreads):
+    return max_threads() if nthreads is None else int(nthreads)
+
+
+def _getrf(prefix, A, m=None, nthreads=None):
+    """In-place LU of a (batch, ncols, ld) column-major batch. Returns (ipiv, info)."""
+    lib = load()
+    dt = np.float64 if prefix == "d" else np.float32
+    assert A.dtype == dt and A.flags.c_contiguous and A.ndim == 3
+    b, n, ld = A.shape
+    m = ld if m is None else m
+    mn = max(min(m, n), 1)
+    ipiv = np.zeros((b, mn), dtype=np.int32)
+    info = np.zeros((b,), dtype=np.int32)
+    fn = getattr(lib, f"oracle_{prefix}getrf_batched")
+    fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_long,
+                   C.c_void_p, C.c_int, C.c_int]
+    fn(m, n, _p(A), ld, n * ld, _p(ipiv), mn, _p(info), b, _threads(nthreads))
+    return ipiv, info
+
+
+def _getrs(prefix, LU, ipiv, B, trans=False, nthreads=None):
+    lib = load()
+    dt = np.float64 if prefix == "d" else np.float32
+    assert LU.dtype == dt and B.dtype == dt and B.flags.c_contiguous
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    b, n, ld = LU.shape
+    nrhs, ldb = B.shape[1], B.shape[2]
+    fn = getattr(lib, f"oracle_{prefix}getrs_batched")
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_long, C.c_void_p,
+                   C.c_long, C.c_void_p, C.c_int, C.c_long, C.c_int, C.c_int]
+    fn(1 if trans else 0, n, nrhs, _p(LU), ld, n * ld, _p(ipiv), ipiv.shape[1], _p(B), ldb,
+       nrhs * ldb, b, _threads(nthreads))
+    return B
+
+
+def _gesv(prefix, A, B, nthreads=None):
+    lib = load()
+    dt = np.float64 if prefix == "d" else np.float32
+    assert A.dtype == dt and B.dtype == dt and A.flags.c_contiguous and B.flags.c_contiguous
+    b, n, ld = A.shape
+    nrhs, ldb = B.shape[1], B.shape[2]
+    ipiv = np.zeros((b, max(n, 1)), dtype=np.int32)
+    info = np.zeros((b,), dtype=np.int32)
+    fn = getattr(lib, f"oracle_{prefix}gesv_batched")
+    fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_long,
+                   C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_int, C.c_int]
+    fn(n, nrhs, _p(A), ld, n * ld, _p(ipiv), ipiv.shape[1], _p(B), ldb, nrhs * ldb, _p(info), b,
+       _threads(nthreads))
+    return ipiv, info
+
+
+def dgetrf_batched(A, m=None, nthreads=None):
+    return _getrf("d", A, m, nthreads)
+
+
+def sgetrf_batched(A, m=None, nthreads=None):
+    return _getrf("s", A, m, nthreads)
+
+
+def dgetrs_batched(LU, ipiv, B, trans=False, nthreads=None):
+    return _getrs("d", LU, ipiv, B, trans, nthreads)
+
+
+def sgetrs_batched(LU, ipiv, B, trans=False, nthreads=None):
+    return _getrs("s", LU, ipiv, B, trans, nthreads)
+
+
+def dgesv_batched(A, B, nthreads=None):
+    return _gesv("d", A, B, nthreads)
+
+
+def sgesv_batched(A, B, nthreads=None):
+    return _gesv("s", A, B, nthreads)
+
+
+def dgetrf(A2, m=None):
+    """Single matrix, (ncols, ld) storage."""
+    A = A2[None]
+    ipiv, info = dgetrf_batched(A, m, nthreads=1)
+    return ipiv[0], int(info[0])
+
+
+def sgetrf(A2, m=None):
+    A = A2[None]
+    ipiv, info = sgetrf_batched(A, m, nthreads=1)
+    return ipiv[0], int(info[0])
+
+
+def dgetrs(LU2, ipiv1, B2, trans=False):
+    dgetrs_batched(LU2[None], ipiv1[None], B2[None], trans, nthreads=1)
+    return B2
+
+
+def sgetrs(LU2, ipiv1, B2, trans=False):
+    sgetrs_batched(LU2[None], ipiv1[None], B2[None], trans, nthreads=1)
+    return B2
+
+
+def dgesv_vbatched(ns, nrhss, As, Bs, nthreads=None):
+    """Variable-size batch: lists of (n_k, ld_k) / (nrhs_k, ldb_k) column-major arrays,
+    solved in place.  Returns (list of ipiv arrays, info array)."""
+    lib = load()
+    b = len(ns)
+    offA = np.zeros(b, dtype=np.int64)
+    offB = np.zeros(b, dtype=np.int64)
+    offP = np.zeros(b, dtype=np.int64)
+    lda = np.array([a.shape[1] for a in As], dtype=np.int32)
+    ldb = np.array([x.shape[1] for x in Bs], dtype=np.int32)
+    na = np.array(ns, dtype=np.int32)
+    nr = np.array(nrhss, dtype=np.int32)
+    offA[1:] = np.cumsum([a.size for a in As])[:-1]
+    offB[1:] = np.cumsum([x.size for x in Bs])[:-1]
+    offP[1:] = np.cumsum(na)[:-1]
+    Aflat = np.concatenate([a.ravel() for a in As]).astype(np.float64)
+    Bflat = np.concatenate([x.ravel() for x in Bs]).astype(np.float64)
+    P = np.zeros(max(int(na.sum()), 1), dtype=np.int32)
+    info = np.zeros(b, dtype=np.int32)
+    fn = lib.oracle_dgesv_vbatched
+    fn.argtypes = [C.c_void_p] * 11 + [C.c_int, C.c_int]
+    fn(_p(na), _p(nr), _p(Aflat), _p(offA), _p(lda), _p(P), _p(offP), _p(Bflat), _p(offB),
+       _p(ldb), _p(info), b, _threads(nthreads))
+    for k in range(b):
+        As[k][...] = Aflat[offA[k]:offA[k] + As[k].size].reshape(As[k].shape)
+        Bs[k][...] = Bflat[offB[k]:offB[k] + Bs[k].size].reshape(Bs[k].shape)
+    pivs = [P[offP[k]:offP[k] + ns[k]].copy() for k in range(b)]
+    return pivs, info

@@ -1,0 +1,86 @@
+"""C-ABI checks that need no GPU: the library builds, loads and exports every
+routine include/magma_lu.h declares; argument errors are reported the MAGMA
+way (negative return, no device work) before any CUDA call."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADERS = sorted((ROOT / "include").glob("*.h"))
+
+
+def declared_functions():
+    names = set()
+    for h in HEADERS:
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = "\n".join(l for l in text.splitlines() if not l.lstrip().startswith("#"))
+        for m in re.finditer(r"\b(magma\w*)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from magma_gb300 import lib as L
+    return L.load()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ("magma_dgetrf_batched", "magma_dgetrs_batched", "magma_dgesv_batched",
+                     "magma_queue_create_internal", "magma_sgetrf_batched"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    from magma_gb300 import lib as L
+    assert set(declared_functions()) <= set(L.exported_names())
+
+
+@pytest.mark.parametrize("args,code", [
+    ((-1, 1, 1, 1), -1),
+    ((4, -1, 4, 4), -2),
+    ((4, 1, 3, 4), -4),
+    ((4, 1, 4, 3), -6),
+])
+def test_gesv_argument_errors(lib, args, code, capfd):
+    n, nrhs, ldda, lddb = args
+    rc = lib.magma_dgesv_batched(n, nrhs, None, ldda, None, None, lddb, None, 1, None)
+    assert rc == code
+    assert "magma_dgesv_batched" in capfd.readouterr().err
+
+
+@pytest.mark.parametrize("args,code", [((-1, 1, 1), -1), ((1, -1, 1), -2), ((5, 5, 4), -4)])
+def test_getrf_argument_errors(lib, args, code):
+    m, n, ldda = args
+    assert lib.magma_dgetrf_batched(m, n, None, ldda, None, None, 1, None) == code
+    assert lib.magma_sgetrf_batched(m, n, None, ldda, None, None, 1, None) == code
+
+
+@pytest.mark.parametrize("args,code", [
+    ((110, 4, 1, 4, 4), -1), ((111, -1, 1, 4, 4), -2), ((112, 4, -1, 4, 4), -3),
+    ((111, 4, 1, 3, 4), -5), ((113, 4, 1, 4, 3), -8)])
+def test_getrs_argument_errors(lib, args, code):
+    trans, n, nrhs, ldda, lddb = args
+    assert lib.magma_dgetrs_batched(trans, n, nrhs, None, ldda, None, None, lddb, 1, None) == code
+
+
+def test_quick_returns_do_no_work(lib):
+    # n == 0 or batchCount == 0 return 0 without touching any pointer
+    assert lib.magma_dgesv_batched(0, 1, None, 1, None, None, 1, None, 5, None) == 0
+    assert lib.magma_dgetrf_batched(4, 4, None, 4, None, None, 0, None) == 0
+    assert lib.magma_dgetrs_batched(111, 4, 0, None, 4, None, None, 4, 3, None) == 0
+
+
+def test_small_path_declines_large_sizes(lib):
+    # magma_?gesv_batched_small returns -100 ("not applicable") like MAGMA
+    assert lib.magma_dgesv_batched_small(33, 1, None, 33, None, None, 33, None, 1, None) == -100
+    assert lib.magma_dgesv_batched_small(8, 17, None, 8, None, None, 8, None, 1, None) == -100
