@@ -280,6 +280,12 @@ def run_ours(args, wl):
     for i in range(args.warmup):
         call(i)
     torch.cuda.synchronize(dev)
+    if args.profile:
+        # profiling mode: only the timed launches, nothing else (for ncu captures)
+        for k in range(args.steps):
+            call(args.warmup + k)
+        torch.cuda.synchronize(dev)
+        return 0
 
     # peaks for the roofline denominators, measured on this device
     probe = C.CDLL(str(ROOT / "magma_gb300" / "libmlu_probe.so"))
@@ -398,6 +404,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="gesv32", choices=sorted(WORKLOADS))
+    ap.add_argument("--profile", action="store_true",
+                    help="run warm-up and timed launches only (for ncu), print nothing")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]()
     if args.impl == "reference":

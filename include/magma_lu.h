@@ -217,6 +217,49 @@ magma_int_t magma_sgesv_batched_small(magma_int_t n, magma_int_t nrhs,
                                       magma_int_t *dinfo_array,
                                       magma_int_t batchCount, magma_queue_t queue);
 
+/* ------------------------------------------------------------------------ */
+/* Batched mixed-precision iterative refinement.  MAGMA refines one matrix
+ * at a time (magma_dsgesv_gpu, src/zcgesv_gpu.cpp:144-366, declared in
+ * include/magma_zc.h); these apply the same algorithm, arguments and ITER
+ * codes to a batch:
+ *   iter[k] >= 0   converged after iter[k] refinements (0: the FP32 solve was
+ *                  already accurate), A_k unchanged, ipiv_k = FP32 pivots;
+ *   iter[k] = -2   A_k overflows in FP32;  -3  the FP32 LU hit a zero pivot;
+ *   iter[k] = -itermax-1  no convergence.
+ * For iter[k] < 0 the matrix is re-solved in FP64 (A_k overwritten by its
+ * FP64 LU, info[k] from that factorisation), like zcgesv_gpu.cpp:352-362. */
+
+/* FP32 factorisation, FP64 residual, ITERMAX = 30, dsgesv stopping rule
+ * ||r_c||_inf <= ||x_c||_inf * ||A||_inf * eps * sqrt(n) for every column c.
+ * Uses (and grows) the queue's workspace; synchronises the queue's stream
+ * once at the end to decide whether any matrix needs the FP64 re-solve.
+ * nrhs <= 16. */
+magma_int_t magma_dsgesv_batched(magma_int_t n, magma_int_t nrhs,
+                                 double **dA_array, magma_int_t ldda,
+                                 magma_int_t **dipiv_array,
+                                 double **dB_array, magma_int_t lddb,
+                                 double **dX_array, magma_int_t lddx,
+                                 magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                 magma_int_t batchCount, magma_queue_t queue);
+
+/* Expert form with caller-provided workspace (work == NULL: *lwork receives
+ * the byte count and nothing else happens; the query needs no queue).
+ * tol > 0 replaces the dsgesv rule by the scaled-residual rule
+ * ||B - A X||_inf / (||A||_inf ||X||_inf n eps) <= tol (the reference tester's
+ * acceptance metric, testing/testing_zgesv_batched.cpp:131-152).
+ * fallback = 0 skips the FP64 re-solve: the call then never synchronises and
+ * is capturable in a CUDA graph; matrices with iter < 0 keep the last iterate.
+ * Returns -15 when *lwork is too small. */
+magma_int_t magma_dsgesv_batched_work(magma_int_t n, magma_int_t nrhs,
+                                      double **dA_array, magma_int_t ldda,
+                                      magma_int_t **dipiv_array,
+                                      double **dB_array, magma_int_t lddb,
+                                      double **dX_array, magma_int_t lddx,
+                                      magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                      magma_int_t itermax, double tol, magma_int_t fallback,
+                                      void *work, size_t *lwork,
+                                      magma_int_t batchCount, magma_queue_t queue);
+
 #ifdef __cplusplus
 }
 #endif

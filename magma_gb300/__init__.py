@@ -6,8 +6,8 @@ ctypes binding (`lib`), tensor-level wrappers (`batched`) and seeded input
 generators (`testing`).
 """
 from . import lib  # noqa: F401
-from .batched import (Queue, colmajor, from_colmajor, gesv_batched, getrf_batched,  # noqa: F401
-                      getrs_batched, ptr_array)
+from .batched import (Queue, colmajor, dsgesv_batched, dsgesv_workspace_bytes,  # noqa: F401
+                      from_colmajor, gesv_batched, getrf_batched, getrs_batched, ptr_array)
 
 __all__ = ["lib", "Queue", "colmajor", "from_colmajor", "ptr_array", "getrf_batched",
-           "getrs_batched", "gesv_batched"]
+           "getrs_batched", "gesv_batched", "dsgesv_batched", "dsgesv_workspace_bytes"]

@@ -101,7 +101,9 @@ def _vp(t: torch.Tensor) -> C.c_void_p:
 
 
 def _check_storage(S: torch.Tensor, name: str):
-    if not S.is_cuda or S.dim() != 3 or S.stride(2) != 1 or S.stride(1) != S.shape[2]:
+    ok = S.is_cuda and S.dim() == 3 and (S.shape[2] <= 1 or S.stride(2) == 1) and \
+        (S.shape[1] <= 1 or S.stride(1) == S.shape[2])
+    if not ok:
         raise ValueError(f"{name} must be CUDA column-major storage (batch, ncols, ld), contiguous")
 
 
@@ -117,6 +119,7 @@ def getrf_batched(S: torch.Tensor, m: int | None = None, ipiv: torch.Tensor | No
     q = queue or Queue.current(S.device)
     lib = _L.load()
     p = _prefix(S)
+    # the pointer arrays must stay referenced until the call has enqueued its kernels
     dA = ptr_array(S)
     dP = ptr_array(ipiv)
     rc = getattr(lib, f"magma_{p}getrf_batched")(m, n, _vp(dA), ld, _vp(dP), _vp(info), b, q.handle)
@@ -135,9 +138,9 @@ def getrs_batched(LU: torch.Tensor, ipiv: torch.Tensor, B: torch.Tensor, trans: 
     lib = _L.load()
     p = _prefix(LU)
     tr = _L.MagmaTrans if trans else _L.MagmaNoTrans
-    rc = getattr(lib, f"magma_{p}getrs_batched")(
-        tr, n, nrhs, _vp(ptr_array(LU)), ld, _vp(ptr_array(ipiv)),
-        _vp(ptr_array(B)), ldb, b, q.handle)
+    dA, dP, dB = ptr_array(LU), ptr_array(ipiv), ptr_array(B)
+    rc = getattr(lib, f"magma_{p}getrs_batched")(tr, n, nrhs, _vp(dA), ld, _vp(dP), _vp(dB), ldb,
+                                                 b, q.handle)
     _check(rc, f"magma_{p}getrs_batched")
     return B
 
@@ -154,8 +157,54 @@ def gesv_batched(S: torch.Tensor, B: torch.Tensor, ipiv: torch.Tensor | None = N
     q = queue or Queue.current(S.device)
     lib = _L.load()
     p = _prefix(S)
-    rc = getattr(lib, f"magma_{p}gesv_batched")(
-        n, nrhs, _vp(ptr_array(S)), ld, _vp(ptr_array(ipiv)), _vp(ptr_array(B)),
-        ldb, _vp(info), b, q.handle)
+    dA, dP, dB = ptr_array(S), ptr_array(ipiv), ptr_array(B)
+    rc = getattr(lib, f"magma_{p}gesv_batched")(n, nrhs, _vp(dA), ld, _vp(dP), _vp(dB), ldb,
+                                                _vp(info), b, q.handle)
     _check(rc, f"magma_{p}gesv_batched")
     return ipiv, info
+
+
+def dsgesv_batched(S: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = None,
+                   itermax: int = 30, tol: float = 0.0, fallback: bool = True,
+                   ipiv: torch.Tensor | None = None, info: torch.Tensor | None = None,
+                   iters: torch.Tensor | None = None, work: torch.Tensor | None = None,
+                   queue: Queue | None = None):
+    """Batched FP32-factor / FP64-refinement solve (magma_dsgesv_batched_work).
+
+    S and B are FP64 column-major storage and are left unchanged unless a
+    matrix falls back to FP64 (then S holds its FP64 LU).  Returns
+    (X, ipiv, info, iters).  `work` may be a preallocated uint8 CUDA tensor of
+    at least dsgesv_workspace_bytes() bytes."""
+    _check_storage(S, "S")
+    _check_storage(B, "B")
+    if S.dtype != torch.float64 or B.dtype != torch.float64:
+        raise TypeError("dsgesv_batched takes float64 inputs")
+    b, n, ld = S.shape
+    nrhs, ldb = B.shape[1], B.shape[2]
+    X = torch.empty_like(B) if X is None else X
+    _check_storage(X, "X")
+    ipiv = torch.empty((b, max(n, 1)), dtype=torch.int32, device=S.device) if ipiv is None else ipiv
+    info = torch.empty((b,), dtype=torch.int32, device=S.device) if info is None else info
+    iters = torch.empty((b,), dtype=torch.int32, device=S.device) if iters is None else iters
+    q = queue or Queue.current(S.device)
+    lib = _L.load()
+    need = dsgesv_workspace_bytes(n, nrhs, b)
+    if work is None or work.numel() < need:
+        work = torch.empty((max(need, 1),), dtype=torch.uint8, device=S.device)
+    lw = C.c_size_t(work.numel())
+    dA, dP, dB, dX = ptr_array(S), ptr_array(ipiv), ptr_array(B), ptr_array(X)
+    rc = lib.magma_dsgesv_batched_work(n, nrhs, _vp(dA), ld, _vp(dP), _vp(dB), ldb, _vp(dX),
+                                       X.shape[2], _vp(info), _vp(iters), itermax, float(tol),
+                                       1 if fallback else 0, _vp(work), C.byref(lw), b, q.handle)
+    _check(rc, "magma_dsgesv_batched_work")
+    return X, ipiv, info, iters
+
+
+def dsgesv_workspace_bytes(n: int, nrhs: int, batch: int) -> int:
+    lib = _L.load()
+    lw = C.c_size_t(0)
+    rc = lib.magma_dsgesv_batched_work(n, nrhs, None, max(n, 1), None, None, max(n, 1), None,
+                                       max(n, 1), None, None, 30, 0.0, 0, None, C.byref(lw),
+                                       batch, None)
+    _check(rc, "magma_dsgesv_batched_work(query)")
+    return int(lw.value)

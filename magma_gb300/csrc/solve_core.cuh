@@ -1,0 +1,193 @@
+// solve_core.cuh -- blocked triangular solves on right-hand sides held in
+// shared memory, shared by getrs (lu_blocked.cu) and the iterative-refinement
+// correction solve (ir.cu).
+//
+// sB holds NR right-hand sides of length n (column c at sB + c*n).  Triangular
+// blocks of 32 rows are solved by warp 0 with shuffles, the remaining rows are
+// then updated by all threads; every element receives its updates in the
+// order of the CPU oracle (oracle/lu_oracle.c, getrs), so results are
+// bit-identical to it.  Must be called by all threads of the block; ends with
+// a __syncthreads.
+#pragma once
+#include "common.cuh"
+
+namespace mlu {
+
+template <typename T, bool TRANS, int SOLVE_NR>
+__device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, int nr)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (!TRANS) {
+        if (tid < nr) {
+            T *b = sB + tid * n;
+            for (int k = 0; k < n; k++) {
+                const int p = ipiv[k] - 1;
+                if (p != k) { T t = b[k]; b[k] = b[p]; b[p] = t; }
+            }
+        }
+        __syncthreads();
+        // forward: L y = b
+        for (int t0 = 0; t0 < n; t0 += 32) {
+            const int tb = min(32, n - t0);
+            if (warp == 0) {
+                T y[SOLVE_NR];
+                const bool v = lane < tb;
+                const T *Lc = A + t0 + lane;   // row t0+lane
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
+                for (int t = 0; t < tb; t++) {
+                    const T l = v ? Lc[(size_t)(t0 + t) * ldda] : T(0);
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++) {
+                        const T yt = __shfl_sync(FULL, y[c], t);
+                        if (v && lane > t) y[c] = Prec<T>::fma_(-l, yt, y[c]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) if (v) sB[c * n + t0 + lane] = y[c];
+            }
+            __syncthreads();
+            for (int i = t0 + tb + tid; i < n; i += blockDim.x) {
+                T acc[SOLVE_NR];
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
+                for (int t = 0; t < tb; t++) {
+                    const T l = A[i + (size_t)(t0 + t) * ldda];
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++)
+                        acc[c] = Prec<T>::fma_(-l, sB[c * n + t0 + t], acc[c]);
+                }
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) sB[c * n + i] = acc[c];
+            }
+            __syncthreads();
+        }
+        // backward: U x = y
+        for (int t1 = n; t1 > 0; t1 -= 32) {
+            const int t0 = max(0, t1 - 32), tb = t1 - t0;
+            if (warp == 0) {
+                T y[SOLVE_NR];
+                const bool v = lane < tb;
+                const T *Ur = A + t0 + lane;
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
+                for (int t = tb - 1; t >= 0; t--) {
+                    const T u = v ? Ur[(size_t)(t0 + t) * ldda] : T(0);   // U(t0+lane, t0+t)
+                    const T d = __shfl_sync(FULL, u, t);
+                    const T r = T(1) / d;
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++) {
+                        const T x = rscale(__shfl_sync(FULL, y[c], t), d, r);
+                        if (lane == t) y[c] = x;
+                        else if (v && lane < t) y[c] = Prec<T>::fma_(-u, x, y[c]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) if (v) sB[c * n + t0 + lane] = y[c];
+            }
+            __syncthreads();
+            for (int i = tid; i < t0; i += blockDim.x) {
+                T acc[SOLVE_NR];
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
+                for (int t = tb - 1; t >= 0; t--) {
+                    const T u = A[i + (size_t)(t0 + t) * ldda];
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++)
+                        acc[c] = Prec<T>::fma_(-u, sB[c * n + t0 + t], acc[c]);
+                }
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) sB[c * n + i] = acc[c];
+            }
+            __syncthreads();
+        }
+    } else {
+        // U^T y = b (forward), U(t,i) = A[t + i*ldda]
+        for (int t0 = 0; t0 < n; t0 += 32) {
+            const int tb = min(32, n - t0);
+            if (warp == 0) {
+                T y[SOLVE_NR];
+                const bool v = lane < tb;
+                const T *Ucol = A + (size_t)(t0 + lane) * ldda;   // column t0+lane
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
+                for (int t = 0; t < tb; t++) {
+                    const T u = v ? Ucol[t0 + t] : T(0);          // U(t0+t, t0+lane)
+                    const T d = __shfl_sync(FULL, u, t);
+                    const T r = T(1) / d;
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++) {
+                        const T x = rscale(__shfl_sync(FULL, y[c], t), d, r);
+                        if (lane == t) y[c] = x;
+                        else if (v && lane > t) y[c] = Prec<T>::fma_(-u, x, y[c]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) if (v) sB[c * n + t0 + lane] = y[c];
+            }
+            __syncthreads();
+            for (int i = t0 + tb + tid; i < n; i += blockDim.x) {
+                T acc[SOLVE_NR];
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
+                const T *Ucol = A + (size_t)i * ldda + t0;
+                for (int t = 0; t < tb; t++) {
+                    const T u = Ucol[t];
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++)
+                        acc[c] = Prec<T>::fma_(-u, sB[c * n + t0 + t], acc[c]);
+                }
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) sB[c * n + i] = acc[c];
+            }
+            __syncthreads();
+        }
+        // L^T x = y (backward), L(t,i) = A[t + i*ldda] for t > i
+        for (int t1 = n; t1 > 0; t1 -= 32) {
+            const int t0 = max(0, t1 - 32), tb = t1 - t0;
+            if (warp == 0) {
+                T y[SOLVE_NR];
+                const bool v = lane < tb;
+                const T *Lcol = A + (size_t)(t0 + lane) * ldda;
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
+                for (int t = tb - 1; t >= 0; t--) {
+                    const T l = v ? Lcol[t0 + t] : T(0);          // L(t0+t, t0+lane)
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++) {
+                        const T x = __shfl_sync(FULL, y[c], t);
+                        if (v && lane < t) y[c] = Prec<T>::fma_(-l, x, y[c]);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) if (v) sB[c * n + t0 + lane] = y[c];
+            }
+            __syncthreads();
+            for (int i = tid; i < t0; i += blockDim.x) {
+                T acc[SOLVE_NR];
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
+                const T *Lcol = A + (size_t)i * ldda + t0;
+                for (int t = tb - 1; t >= 0; t--) {
+                    const T l = Lcol[t];
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++)
+                        acc[c] = Prec<T>::fma_(-l, sB[c * n + t0 + t], acc[c]);
+                }
+#pragma unroll
+                for (int c = 0; c < SOLVE_NR; c++) sB[c * n + i] = acc[c];
+            }
+            __syncthreads();
+        }
+        if (tid < nr) {
+            T *b = sB + tid * n;
+            for (int k = n - 1; k >= 0; k--) {
+                const int p = ipiv[k] - 1;
+                if (p != k) { T t = b[k]; b[k] = b[p]; b[p] = t; }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace mlu

@@ -198,3 +198,111 @@ int oracle_max_threads(void)
     return 1;
 #endif
 }
+
+/* Batched mixed-precision iterative refinement, one matrix: the restatement of
+ * magma_dsgesv_gpu (src/zcgesv_gpu.cpp:144-366) in the exact arithmetic order
+ * of the GPU implementation:
+ *   anrm = max_i sum_j |a_ij| (j ascending); As = (float)A (overflow: iter -2);
+ *   sgetrf(As) (info > 0: iter -3); X = 0, R = B;
+ *   solve: X = X + (double)sgetrs(As, (float)R);
+ *   residual: r_i = b_i, r_i = fma(-a_ij, x_j, r_i) for j ascending;
+ *   norms: per column max|r|, max|x|; row sums over the columns (ascending);
+ *   stop when every column has max|r_c| <= max|x_c| * anrm*eps*sqrt(n)
+ *   (tol <= 0) or when rowmax|R| <= tol * (anrm * rowmax|X| * n * eps);
+ *   checks after the initial solve (iter 0) and after each of itermax
+ *   refinements; not converged: iter = -itermax-1.  When iter < 0 and
+ *   fallback is set, A is overwritten by its FP64 LU and X solved in FP64.
+ * Returns info. */
+int oracle_dsgesv(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
+                  int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out)
+{
+    const double eps = 1.1102230246251565e-16;
+    double anrm = 0.0;
+    int ovf = 0;
+    float *As = (float *)malloc(sizeof(float) * (size_t)n * n + 4);
+    float *Rs = (float *)malloc(sizeof(float) * (size_t)n * nrhs + 4);
+    double *R = (double *)malloc(sizeof(double) * (size_t)n * nrhs + 8);
+    for (int i = 0; i < n; i++) {
+        double rs = 0.0;
+        for (int j = 0; j < n; j++) {
+            double a = A[i + (size_t)j * lda];
+            rs += fabs(a);
+            float f = (float)a;
+            if (isinf(f) && !isinf(a)) ovf = 1;
+            As[i + (size_t)j * n] = f;
+        }
+        if (rs > anrm) anrm = rs;
+    }
+    int iter = 0, info = 0, state = 0;   /* 0 active, 1 converged, 2 failed */
+    if (ovf) { iter = -2; state = 2; }
+    int sinfo = oracle_sgetrf(n, n, As, n, ipiv);
+    if (state == 0 && sinfo > 0) { iter = -3; state = 2; }
+    for (int c = 0; c < nrhs; c++)
+        for (int i = 0; i < n; i++) {
+            R[i + (size_t)c * n] = B[i + (size_t)c * ldb];
+            X[i + (size_t)c * ldx] = 0.0;
+        }
+    for (int it = -1; state == 0 && it <= itermax; it++) {
+        if (it >= 0) {
+            /* norms of the residual computed at the end of the previous pass */
+            double rrow = 0.0, xrow = 0.0;
+            int ok = 1;
+            double cte = anrm * eps * sqrt((double)n);
+            for (int c = 0; c < nrhs; c++) {
+                double rc = 0.0, xc = 0.0;
+                for (int i = 0; i < n; i++) {
+                    double ra = fabs(R[i + (size_t)c * n]), xa = fabs(X[i + (size_t)c * ldx]);
+                    if (ra > rc) rc = ra;
+                    if (xa > xc) xc = xa;
+                }
+                if (!(rc <= xc * cte)) ok = 0;
+            }
+            for (int i = 0; i < n; i++) {
+                double rs = 0.0, xs = 0.0;
+                for (int c = 0; c < nrhs; c++) {
+                    rs += fabs(R[i + (size_t)c * n]);
+                    xs += fabs(X[i + (size_t)c * ldx]);
+                }
+                if (rs > rrow) rrow = rs;
+                if (xs > xrow) xrow = xs;
+            }
+            if (tol > 0.0) ok = rrow <= tol * (anrm * xrow * (double)n * eps);
+            if (ok) { state = 1; iter = it; break; }
+            if (it == itermax) { state = 2; iter = -itermax - 1; break; }
+        }
+        for (size_t e = 0; e < (size_t)n * nrhs; e++) Rs[e] = (float)R[e];
+        oracle_sgetrs(0, n, nrhs, As, n, ipiv, Rs, n);
+        for (int c = 0; c < nrhs; c++)
+            for (int i = 0; i < n; i++)
+                X[i + (size_t)c * ldx] = X[i + (size_t)c * ldx] + (double)Rs[i + (size_t)c * n];
+        for (int c = 0; c < nrhs; c++)
+            for (int i = 0; i < n; i++) {
+                double acc = B[i + (size_t)c * ldb];
+                for (int j = 0; j < n; j++)
+                    acc = fma(-A[i + (size_t)j * lda], X[j + (size_t)c * ldx], acc);
+                R[i + (size_t)c * n] = acc;
+            }
+    }
+    if (state == 2 && fallback) {
+        info = oracle_dgetrf(n, n, A, lda, ipiv);
+        for (int c = 0; c < nrhs; c++)
+            for (int i = 0; i < n; i++) X[i + (size_t)c * ldx] = B[i + (size_t)c * ldb];
+        oracle_dgetrs(0, n, nrhs, A, lda, ipiv, X, ldx);
+    }
+    free(As); free(Rs); free(R);
+    *iter_out = iter;
+    return info;
+}
+
+void oracle_dsgesv_batched(int n, int nrhs, double *A, int lda, long strideA, const double *B,
+                           int ldb, long strideB, double *X, int ldx, long strideX, int *ipiv,
+                           long strideP, int *info, int *iter, int itermax, double tol,
+                           int fallback, int batch, int nthreads)
+{
+    (void)nthreads;
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+    for (int k = 0; k < batch; k++)
+        info[k] = oracle_dsgesv(n, nrhs, A + k * strideA, lda, B + k * strideB, ldb,
+                                X + k * strideX, ldx, ipiv + k * strideP, itermax, tol, fallback,
+                                iter + k);
+}

@@ -179,3 +179,25 @@ def dgesv_vbatched(ns, nrhss, As, Bs, nthreads=None):
         Bs[k][...] = Bflat[offB[k]:offB[k] + Bs[k].size].reshape(Bs[k].shape)
     pivs = [P[offP[k]:offP[k] + ns[k]].copy() for k in range(b)]
     return pivs, info
+
+
+def dsgesv_batched(A, B, itermax=30, tol=0.0, fallback=True, nthreads=None):
+    """Mixed-precision IR restatement (oracle_dsgesv).  A: (batch, n, ld) FP64
+    storage, modified only for matrices that fall back; B: (batch, nrhs, ldb).
+    Returns (X, ipiv, info, iters) with X of B's shape."""
+    lib = load()
+    assert A.dtype == np.float64 and B.dtype == np.float64
+    b, n, ld = A.shape
+    nrhs, ldb = B.shape[1], B.shape[2]
+    X = np.zeros_like(B)
+    ipiv = np.zeros((b, max(n, 1)), dtype=np.int32)
+    info = np.zeros((b,), dtype=np.int32)
+    iters = np.zeros((b,), dtype=np.int32)
+    fn = lib.oracle_dsgesv_batched
+    fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_int, C.c_long,
+                   C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p,
+                   C.c_int, C.c_double, C.c_int, C.c_int, C.c_int]
+    fn(n, nrhs, _p(A), ld, n * ld, _p(B), ldb, nrhs * ldb, _p(X), ldb, nrhs * ldb, _p(ipiv),
+       ipiv.shape[1], _p(info), _p(iters), itermax, float(tol), 1 if fallback else 0, b,
+       _threads(nthreads))
+    return X, ipiv, info, iters

@@ -1,0 +1,129 @@
+"""GPU parity for the batched mixed-precision iterative refinement
+(magma_dsgesv_batched_work) against the oracle's restatement of
+magma_dsgesv_gpu: iterates, iteration counts (ITER codes), pivots and info are
+bit-identical; solutions are FP64-accurate.
+
+Edge cases follow src/zcgesv_gpu.cpp: FP32 overflow (iter -2), singular FP32
+factor (iter -3), no convergence (iter -itermax-1), each followed by the FP64
+re-solve."""
+import numpy as np
+import pytest
+import torch
+
+import magma_gb300 as mg
+import oracle
+from magma_gb300.testing import svd_batch_torch
+from tests.util import from_storage, scaled_residual, to_storage
+
+pytestmark = pytest.mark.gpu
+
+
+def _svd(batch, n, kappas, seed):
+    return svd_batch_torch(batch, n, kappas, seed, device="cpu").numpy()
+
+
+def _run_both(A, Bm, cuda, itermax=30, tol=0.0, fallback=True):
+    n = A.shape[1]
+    S, Bs = to_storage(A), to_storage(Bm)
+    rS = S.copy()
+    rX, ripiv, rinfo, riters = oracle.dsgesv_batched(rS, Bs, itermax=itermax, tol=tol,
+                                                     fallback=fallback)
+    dS = torch.from_numpy(S).to(cuda)
+    dB = torch.from_numpy(Bs).to(cuda)
+    X, ipiv, info, iters = mg.dsgesv_batched(dS, dB, itermax=itermax, tol=tol, fallback=fallback)
+    torch.cuda.synchronize()
+    gpu = (X.cpu().numpy(), ipiv.cpu().numpy(), info.cpu().numpy(), iters.cpu().numpy(),
+           dS.cpu().numpy())
+    ref = (rX, ripiv, rinfo, riters, rS)
+    return gpu, ref
+
+
+def _assert_same(gpu, ref, n):
+    X, ipiv, info, iters, S = gpu
+    rX, ripiv, rinfo, riters, rS = ref
+    assert np.array_equal(iters, riters), (iters, riters)
+    assert np.array_equal(info, rinfo)
+    assert np.array_equal(ipiv[:, :n], ripiv[:, :n])
+    assert np.array_equal(X, rX)
+    assert np.array_equal(S, rS)
+
+
+@pytest.mark.parametrize("tol", [0.0, 30.0])
+@pytest.mark.parametrize("n,nrhs", [(20, 1), (64, 4), (100, 9), (160, 16)])
+def test_dsgesv_matches_oracle(cuda, n, nrhs, tol):
+    kappas = [1e2, 1e4, 1e6] * 3
+    A = _svd(9, n, kappas, seed=n)
+    Bm = np.random.default_rng(n).uniform(-1, 1, (9, n, nrhs))
+    gpu, ref = _run_both(A, Bm, cuda, tol=tol)
+    _assert_same(gpu, ref, n)
+    assert np.all(gpu[3] >= 0)
+    res = scaled_residual(A, from_storage(gpu[0], n), Bm)
+    assert res.max() <= 30
+
+
+def test_dsgesv_n512_kappa_mix(cuda):
+    """The refinement workload's shape (n=512, nrhs=4, kappa 1e2/1e4/1e6) on a small batch."""
+    A = _svd(3, 512, [1e2, 1e4, 1e6], seed=5)
+    Bm = np.random.default_rng(5).uniform(-1, 1, (3, 512, 4))
+    gpu, ref = _run_both(A, Bm, cuda, tol=30.0)
+    _assert_same(gpu, ref, 512)
+    assert scaled_residual(A, from_storage(gpu[0], 512), Bm).max() <= 30
+
+
+def test_dsgesv_no_convergence_falls_back(cuda):
+    A = _svd(2, 48, [1e12, 1e2], seed=9)
+    Bm = np.random.default_rng(9).uniform(-1, 1, (2, 48, 2))
+    gpu, ref = _run_both(A, Bm, cuda, itermax=3)
+    _assert_same(gpu, ref, 48)
+    assert gpu[3][0] == -4 and gpu[3][1] >= 0
+    assert not np.array_equal(gpu[4][0], to_storage(A)[0])    # A_0 now holds its FP64 LU
+    assert np.array_equal(gpu[4][1], to_storage(A)[1])        # A_1 untouched
+
+
+def test_dsgesv_overflow_and_singular(cuda):
+    rng = np.random.default_rng(4)
+    A = rng.uniform(-1, 1, (3, 40, 40))
+    A[0, 3, 7] = 1e39          # not representable in FP32
+    A[1, :, 5] = 0.0           # singular in both precisions
+    Bm = rng.uniform(-1, 1, (3, 40, 1))
+    gpu, ref = _run_both(A, Bm, cuda)
+    _assert_same(gpu, ref, 40)
+    assert list(gpu[3][:2]) == [-2, -3]
+    assert gpu[2][1] == 6 and gpu[3][2] >= 0
+
+
+def test_dsgesv_without_fallback_never_syncs_and_reports(cuda):
+    A = _svd(2, 48, [1e12, 1e3], seed=3)
+    Bm = np.random.default_rng(3).uniform(-1, 1, (2, 48, 1))
+    gpu, ref = _run_both(A, Bm, cuda, itermax=2, tol=30.0, fallback=False)
+    _assert_same(gpu, ref, 48)
+    assert gpu[3][0] < 0 and gpu[3][1] >= 0
+    assert np.array_equal(gpu[4], to_storage(A))             # A untouched without fallback
+
+
+def test_dsgesv_public_entry_uses_queue_workspace(cuda):
+    """magma_dsgesv_batched (no _work) grows the queue's workspace itself."""
+    import ctypes as C
+    from magma_gb300 import lib as L
+    from magma_gb300.batched import Queue, ptr_array
+    n, nrhs, b = 70, 3, 5
+    A = _svd(b, n, [1e3] * b, seed=2)
+    Bm = np.random.default_rng(2).uniform(-1, 1, (b, n, nrhs))
+    S, Bs = to_storage(A), to_storage(Bm)
+    rX, ripiv, rinfo, riters = oracle.dsgesv_batched(S.copy(), Bs)
+    dS = torch.from_numpy(S).to(cuda)
+    dB = torch.from_numpy(Bs).to(cuda)
+    dX = torch.empty_like(dB)
+    ipiv = torch.empty((b, n), dtype=torch.int32, device=cuda)
+    info = torch.empty((b,), dtype=torch.int32, device=cuda)
+    iters = torch.empty((b,), dtype=torch.int32, device=cuda)
+    q = Queue.current(cuda)
+    pa, pp, pb, px = ptr_array(dS), ptr_array(ipiv), ptr_array(dB), ptr_array(dX)
+    rc = L.load().magma_dsgesv_batched(n, nrhs, C.c_void_p(pa.data_ptr()), n,
+                                       C.c_void_p(pp.data_ptr()), C.c_void_p(pb.data_ptr()), n,
+                                       C.c_void_p(px.data_ptr()), n, C.c_void_p(info.data_ptr()),
+                                       C.c_void_p(iters.data_ptr()), b, q.handle)
+    torch.cuda.synchronize()
+    assert rc == 0
+    assert np.array_equal(dX.cpu().numpy(), rX)
+    assert np.array_equal(iters.cpu().numpy(), riters)
