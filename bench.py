@@ -1,17 +1,30 @@
 """Benchmark of the batched LU factor-and-solve path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload gesv32]
+                    [--workload dsgesv512|gesv32] [--profile]
 
-A step is one batched factor-and-solve of the workload's whole batch.  Each
-step works on its own pre-filled copy of the inputs (all copies together are
-larger than L2, so no step reads another's data from cache); `value` is
-solves/s with inputs resident in HBM, `e2e` is the same metric through the
-public C-ABI call with pinned host buffers copied in and the solutions and
-info copied out inside the timed region.
+Metric: FP64-accurate batched solves/s -- solves per second that meet the
+reference tester's accuracy bar ||b - A x||_inf / (||A||_inf ||x||_inf n eps)
+<= 30 (testing/testing_zgesv_batched.cpp:131-152).
 
---impl reference times the reference's CPU path (LAPACK-style getrf + getrs
-per matrix under OpenMP, here the C restatement in oracle/) on the host cores.
+Workloads
+  dsgesv512 (default)  512 double matrices n=512, A = U diag(s) V^T with s
+                       geometric from 1 to 1/kappa, kappa in {1e2,1e4,1e6} (a
+                       third each), nrhs=4 uniform(-1,1).  A step is one call of
+                       magma_dsgesv_batched_work (FP32 LU, FP64 residual and
+                       update, stop at scaled residual <= 30 or 30 iterations,
+                       FP64 re-solve of any matrix that does not converge).  The
+                       plain FP64 path (magma_dgesv_batched) is timed on the same
+                       inputs and reported beside it.
+  gesv32               magma_dgesv_batched on 10,000 matrices 32x32, nrhs=1,
+                       uniform(-1,1).
+
+`value` is measured with the inputs resident in HBM (each step reads more
+than L2 holds); `e2e` is the same metric through the C-ABI call with pinned
+host buffers: inputs copied in and solutions + info copied out inside the
+timed region.  --impl reference times the reference's CPU path (LAPACK-style
+dgetrf + dgetrs per matrix under OpenMP: the C restatement in oracle/) on the
+host cores for the same workload.
 """
 from __future__ import annotations
 
@@ -31,8 +44,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-# --------------------------------------------------------------------------
-# workloads
+METRIC = "FP64-accurate batched solves/s"
+EPS = float(np.finfo(np.float64).eps)
 
 
 def flops_getrf(m, n):
@@ -53,35 +66,281 @@ def flops_getrs(n, nrhs):
     return nrhs * n * n + nrhs * n * (n - 1.0)
 
 
+def scaled_residuals(A, X, B):
+    """Per-matrix ||B - A X||_inf / (||A||_inf ||X||_inf n eps), torch, math orientation."""
+    n = A.shape[1]
+    R = A @ X - B
+    return R.abs().sum(2).amax(1) / (A.abs().sum(2).amax(1) * X.abs().sum(2).amax(1) * n * EPS)
+
+
+def vp(t):
+    return C.c_void_p(t.data_ptr())
+
+
+# --------------------------------------------------------------------------
+# workloads
+
+
 class Gesv32:
-    """Plain FP64 magma_dgesv_batched: 10,000 matrices 32x32, one RHS, entries
-    uniform(-1,1) from a seeded generator."""
     name = "gesv32"
     batch, n, nrhs = 10000, 32, 1
-    dtype = "f64"
     seed = 20240601
+    dtype = "f64"
 
     def describe(self):
-        return {"workload": "dgesv_batched n=32 nrhs=1 batch=10000 uniform(-1,1) FP64",
+        return {"workload": "magma_dgesv_batched n=32 nrhs=1 batch=10000 uniform(-1,1) FP64",
                 "batch": self.batch, "n": self.n, "nrhs": self.nrhs, "precision": "fp64",
-                "matrix": "uniform(-1,1)", "l2": "inputs larger than L2: each step owns its copy"}
-
-    def flops_per_solve(self):
-        return flops_getrf(self.n, self.n) + flops_getrs(self.n, self.nrhs)
-
-    def bytes_per_solve(self):
-        # A read+write, B read + X write, ipiv, info, three pointers
-        n, r = self.n, self.nrhs
-        return 16 * n * n + 16 * n * r + 4 * n + 4 + 24
+                "matrix": "uniform(-1,1)",
+                "l2": "inputs larger than L2: each step owns a private 85 MB copy"}
 
     def host_inputs(self):
         from magma_gb300.testing import colmajor_uniform
         S = colmajor_uniform(self.batch, self.n, self.n, self.n, self.seed)
-        X = colmajor_uniform(self.batch, self.nrhs, self.n, self.n, self.seed + 1)
-        return S, X
+        B = colmajor_uniform(self.batch, self.nrhs, self.n, self.n, self.seed + 1)
+        return S, B
+
+    def setup(self, dev, nsteps, lib, q):
+        import torch
+        from magma_gb300.batched import ptr_array
+        S_h, B_h = self.host_inputs()
+        c = {"S_h": S_h, "B_h": B_h}
+        S0 = torch.from_numpy(S_h).to(dev)
+        B0 = torch.from_numpy(B_h).to(dev)
+        c["S0"], c["B0"] = S0, B0
+        c["S"] = [S0.clone() for _ in range(nsteps)]
+        c["X"] = [B0.clone() for _ in range(nsteps)]
+        c["dA"] = [ptr_array(s) for s in c["S"]]
+        c["dX"] = [ptr_array(x) for x in c["X"]]
+        c["ipiv"] = torch.empty((self.batch, self.n), dtype=torch.int32, device=dev)
+        c["info"] = torch.empty((self.batch,), dtype=torch.int32, device=dev)
+        c["dP"] = ptr_array(c["ipiv"])
+        c["lib"], c["q"] = lib, q
+        return c
+
+    def step(self, c, i):
+        rc = c["lib"].magma_dgesv_batched(self.n, self.nrhs, vp(c["dA"][i]), self.n, vp(c["dP"]),
+                                          vp(c["dX"][i]), self.n, vp(c["info"]), self.batch,
+                                          c["q"].handle)
+        if rc != 0:
+            raise RuntimeError(f"magma_dgesv_batched returned {rc}")
+
+    kernels_per_step = 1
+    dominant = "mlu::small_gesv_kernel<double,32,1>"
+
+    def e2e_setup(self, c):
+        import torch
+        c["hS"] = torch.from_numpy(c["S_h"]).pin_memory()
+        c["hB"] = torch.from_numpy(c["B_h"]).pin_memory()
+        c["hX"] = torch.empty_like(c["hB"]).pin_memory()
+        c["hInfo"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
+        h2d = c["hS"].numel() * 8 + c["hB"].numel() * 8
+        d2h = c["hX"].numel() * 8 + c["hInfo"].numel() * 4
+        return h2d, d2h
+
+    def e2e_step(self, c):
+        c["S"][0].copy_(c["hS"], non_blocking=True)
+        c["X"][0].copy_(c["hB"], non_blocking=True)
+        self.step(c, 0)
+        c["hX"].copy_(c["X"][0], non_blocking=True)
+        c["hInfo"].copy_(c["info"], non_blocking=True)
+
+    def accuracy(self, c, last):
+        n = self.n
+        A = c["S0"].transpose(1, 2)
+        X = c["X"][last][:, :, :n].transpose(1, 2)
+        B = c["B0"][:, :, :n].transpose(1, 2)
+        res = scaled_residuals(A, X, B)
+        return int((res <= 30).sum()), float(res.max())
+
+    def flops_per_solve(self):
+        return flops_getrf(self.n, self.n) + flops_getrs(self.n, self.nrhs)
+
+    def roofline(self, step_ms, peaks):
+        flops = self.flops_per_solve() * self.batch
+        n, r = self.n, self.nrhs
+        nbytes = (16 * n * n + 16 * n * r + 4 * n + 4 + 24) * self.batch
+        ach = flops / (step_ms * 1e-3) / 1e12
+        return {"bound": "fp64", "achieved": ach, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["fp64_tflops"], "traffic": _traffic(self.name),
+                "peak_source": "FP64 FMA-throughput probe run inside bench.py "
+                               "(magma_gb300/probe/peaks.cu)",
+                "kernel": self.dominant, "launch_ms": step_ms,
+                "algorithmic_flops_per_launch": flops, "algorithmic_bytes_per_launch": nbytes,
+                "hbm_gbs": nbytes / (step_ms * 1e-3) / 1e9,
+                "hbm_frac_of_measured": nbytes / (step_ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+
+    def cpu_sample(self, nthreads, target_s):
+        import oracle
+        S_h, B_h = self.host_inputs()
+
+        def run(k):
+            s, x = S_h[:k].copy(), B_h[:k].copy()
+            t0 = time.perf_counter()
+            oracle.dgesv_batched(s, x, nthreads=nthreads)
+            return time.perf_counter() - t0
+        k = min(self.batch, 1000)
+        t = run(k)
+        k = int(min(self.batch, max(k, k * target_s / max(t, 1e-6))))
+        ts = [run(k) for _ in range(3)]
+        return k, statistics.median(ts), f"{k} of the {self.batch} matrices"
 
 
-WORKLOADS = {"gesv32": Gesv32}
+class Dsgesv512:
+    name = "dsgesv512"
+    batch, n, nrhs = 512, 512, 4
+    seed = 20240603
+    dtype = "f64 (FP32 factorisation, FP64 residual/update)"
+    tol = 30.0
+    itermax = 30
+
+    def describe(self):
+        return {"workload": "magma_dsgesv_batched_work: 512 FP64 matrices n=512, nrhs=4, "
+                            "A=U diag(s) V^T, kappa in {1e2,1e4,1e6}; FP32 LU + FP64 refinement, "
+                            "stop at scaled residual <= 30 or 30 iterations",
+                "batch": self.batch, "n": self.n, "nrhs": self.nrhs,
+                "precision": "fp32 factor, fp64 residual/update/convergence",
+                "matrix": "svd-type, singular values geometric 1..1/kappa",
+                "compared_with": "magma_dgesv_batched (plain FP64) on the same inputs",
+                "l2": "inputs larger than L2: A is 1 GiB FP64"}
+
+    def gen(self, dev):
+        import torch
+        from magma_gb300.testing import svd_batch_torch
+        kap = [1e2, 1e4, 1e6] * (self.batch // 3 + 1)
+        A = svd_batch_torch(self.batch, self.n, kap[:self.batch], self.seed, device=dev)
+        g = torch.Generator(device="cpu").manual_seed(self.seed + 1)
+        B = (torch.rand((self.batch, self.n, self.nrhs), generator=g, dtype=torch.float64) * 2
+             - 1).to(dev)
+        return A, B
+
+    def setup(self, dev, nsteps, lib, q):
+        import torch
+        import magma_gb300 as mg
+        from magma_gb300.batched import ptr_array
+        A, B = self.gen(dev)
+        c = {"A": A, "Bm": B, "lib": lib, "q": q}
+        c["S"] = A.transpose(1, 2).contiguous()          # column-major storage
+        c["B"] = B.transpose(1, 2).contiguous()
+        c["X"] = torch.empty_like(c["B"])
+        b, n = self.batch, self.n
+        c["ipiv"] = torch.empty((b, n), dtype=torch.int32, device=dev)
+        c["info"] = torch.empty((b,), dtype=torch.int32, device=dev)
+        c["iter"] = torch.empty((b,), dtype=torch.int32, device=dev)
+        c["work"] = torch.empty((mg.dsgesv_workspace_bytes(n, self.nrhs, b),), dtype=torch.uint8,
+                                device=dev)
+        c["lwork"] = C.c_size_t(c["work"].numel())
+        for k in ("S", "B", "X", "ipiv"):
+            c["d" + k] = ptr_array(c[k])
+        return c
+
+    def step(self, c, i):
+        b, n, r = self.batch, self.n, self.nrhs
+        rc = c["lib"].magma_dsgesv_batched_work(
+            n, r, vp(c["dS"]), n, vp(c["dipiv"]), vp(c["dB"]), n, vp(c["dX"]), n, vp(c["info"]),
+            vp(c["iter"]), self.itermax, self.tol, 1, vp(c["work"]), C.byref(c["lwork"]), b,
+            c["q"].handle)
+        if rc != 0:
+            raise RuntimeError(f"magma_dsgesv_batched_work returned {rc}")
+
+    kernels_per_step = None   # set after a run from the launch list
+    dominant = "ir_residual_kernel<4> (FP64 residual)"
+
+    def e2e_setup(self, c):
+        import torch
+        c["hS"] = c["S"].cpu().pin_memory()
+        c["hB"] = c["B"].cpu().pin_memory()
+        c["hX"] = torch.empty_like(c["hB"]).pin_memory()
+        c["hIter"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
+        c["hInfo"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
+        h2d = c["hS"].numel() * 8 + c["hB"].numel() * 8
+        d2h = c["hX"].numel() * 8 + 8 * self.batch
+        return h2d, d2h
+
+    def e2e_step(self, c):
+        c["S"].copy_(c["hS"], non_blocking=True)
+        c["B"].copy_(c["hB"], non_blocking=True)
+        self.step(c, 0)
+        c["hX"].copy_(c["X"], non_blocking=True)
+        c["hIter"].copy_(c["iter"], non_blocking=True)
+        c["hInfo"].copy_(c["info"], non_blocking=True)
+
+    def accuracy(self, c, last):
+        X = c["X"].transpose(1, 2)
+        res = scaled_residuals(c["A"], X, c["Bm"])
+        it = c["iter"].cpu()
+        return int((res <= 30).sum()), float(res.max()), {
+            "iterations_histogram": {str(int(k)): int(v) for k, v in
+                                     zip(*np.unique(it.numpy(), return_counts=True))},
+            "fallbacks": int((it < 0).sum())}
+
+    def fp64_path(self, c, steps, warmup):
+        """Plain FP64 magma_dgesv_batched on the same inputs, private copies per step."""
+        import torch
+        from magma_gb300.batched import ptr_array
+        b, n, r = self.batch, self.n, self.nrhs
+        stream = torch.cuda.current_stream()
+        tot = steps + warmup
+        Ss = [c["S"].clone() for _ in range(tot)]
+        Xs = [c["B"].clone() for _ in range(tot)]
+        dS = [ptr_array(s) for s in Ss]
+        dX = [ptr_array(x) for x in Xs]
+        lib, q = c["lib"], c["q"]
+
+        def call(i):
+            rc = lib.magma_dgesv_batched(n, r, vp(dS[i]), n, vp(c["dipiv"]), vp(dX[i]), n,
+                                         vp(c["info"]), b, q.handle)
+            if rc != 0:
+                raise RuntimeError(f"magma_dgesv_batched returned {rc}")
+        for i in range(warmup):
+            call(i)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(steps):
+            call(warmup + i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        res = scaled_residuals(c["A"], Xs[-1].transpose(1, 2), c["Bm"])
+        n_ok = int((res <= 30).sum())
+        del Ss, Xs
+        return {"value": n_ok / (ms * 1e-3), "unit": "solves/s", "ms_per_step": ms,
+                "max_scaled_residual": float(res.max()), "steps": steps,
+                "call": "magma_dgesv_batched"}
+
+    def roofline(self, step_ms, peaks, phase_ms=None):
+        # dominant kernel: FP64 residual R = B - A X (n*n*nrhs FMA per matrix per pass)
+        return None
+
+    def cpu_sample(self, nthreads, target_s):
+        import oracle
+        if not hasattr(self, "_cpu_inputs"):
+            A, B = self.gen("cpu")
+            self._cpu_inputs = (A.transpose(1, 2).contiguous().numpy(),
+                                B.transpose(1, 2).contiguous().numpy())
+        S, Bs = self._cpu_inputs
+
+        def run(k):
+            s, x = S[:k].copy(), Bs[:k].copy()
+            t0 = time.perf_counter()
+            oracle.dgesv_batched(s, x, nthreads=nthreads)
+            return time.perf_counter() - t0
+        k = max(nthreads, 1)
+        t = run(k)
+        k = int(min(self.batch, max(k, k * target_s / max(t, 1e-6))))
+        ts = [run(k) for _ in range(3)]
+        return k, statistics.median(ts), f"{k} of the {self.batch} matrices (FP64 dgetrf+dgetrs)"
+
+
+WORKLOADS = {"dsgesv512": Dsgesv512, "gesv32": Gesv32}
+
+
+def _traffic(name):
+    f = ROOT / "profiles" / "traffic.json"
+    if f.exists():
+        return json.loads(f.read_text()).get(name)
+    return None
+
 
 # --------------------------------------------------------------------------
 # helpers
@@ -144,8 +403,8 @@ def dist_setup():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pg = None
     if world > 1:
-        import torch.distributed as dist
         import torch
+        import torch.distributed as dist
         backend = "nccl" if torch.cuda.is_available() else "gloo"
         dist.init_process_group(backend)
         pg = dist
@@ -154,8 +413,7 @@ def dist_setup():
 
 def barrier(pg, dev=None):
     if pg is not None:
-        import torch
-        if dev is not None:
+        if dev is not None and dev.type == "cuda":
             pg.barrier(device_ids=[dev.index])
         else:
             pg.barrier()
@@ -170,36 +428,33 @@ def allmax(pg, x, dev):
     return float(t.item())
 
 
+def measured_peaks(stream_handle):
+    probe = C.CDLL(str(ROOT / "magma_gb300" / "libmlu_probe.so"))
+    for f in ("mlu_probe_fp64_tflops", "mlu_probe_fp32_tflops"):
+        getattr(probe, f).restype = C.c_double
+        getattr(probe, f).argtypes = [C.c_void_p]
+    p = {"fp64_tflops": probe.mlu_probe_fp64_tflops(C.c_void_p(stream_handle)),
+         "fp32_tflops": probe.mlu_probe_fp32_tflops(C.c_void_p(stream_handle))}
+    f = ROOT / "MEASURED_PEAKS.json"
+    d = json.loads(f.read_text()) if f.exists() else {}
+    p["hbm_gbs"] = d.get("hbm_gbs", 6800.0)
+    p["hbm_source"] = "MEASURED_PEAKS.json" if "hbm_gbs" in d else "fallback 6800 GB/s"
+    p["bf16_tflops"] = d.get("bf16_tflops", 1900.0)
+    return p
+
+
 # --------------------------------------------------------------------------
 # CPU reference leg
-
-
-def cpu_run(wl, sample, nthreads):
-    """Time oracle gesv (C, OpenMP over the batch) on `sample` matrices.  Returns
-    seconds for one pass (median of 3) and the thread count."""
-    import oracle
-    S, X = wl.host_inputs()
-    S, X = S[:sample].copy(), X[:sample].copy()
-    times = []
-    for _ in range(3):
-        s, x = S.copy(), X.copy()
-        t0 = time.perf_counter()
-        oracle.dgesv_batched(s, x, nthreads=nthreads)
-        times.append(time.perf_counter() - t0)
-    return statistics.median(times), nthreads
 
 
 def cpu_baseline(wl, target_s=3.0):
     import oracle
     nthreads = oracle.max_threads()
-    probe = min(wl.batch, 500)
-    t, _ = cpu_run(wl, probe, nthreads)
-    sample = int(min(wl.batch, max(probe, probe * target_s / max(t, 1e-6) / 3)))
-    t, _ = cpu_run(wl, sample, nthreads)
-    return {"value": sample / t, "unit": "solves/s", "cores": nthreads, "kind": "port",
-            "sample": f"{sample} of the {wl.batch} matrices of the workload, oracle/lu_oracle.c "
-                      f"getrf+getrs per matrix, OpenMP schedule(dynamic) over {nthreads} threads, "
-                      f"median of 3 passes"}
+    k, t, what = wl.cpu_sample(nthreads, target_s)
+    return {"value": k / t, "unit": "solves/s", "cores": nthreads, "kind": "port",
+            "sample": f"{what}: oracle/lu_oracle.c dgetrf+dgetrs per matrix (the reference's "
+                      f"CPU path, testing/testing_zgesv_batched.cpp:160-176, restated), OpenMP "
+                      f"schedule(dynamic) over {nthreads} threads, median of 3 passes"}
 
 
 def run_reference(args, wl):
@@ -208,28 +463,24 @@ def run_reference(args, wl):
         return 0
     import oracle
     nthreads = oracle.max_threads()
-    probe = min(wl.batch, 500)
-    t, _ = cpu_run(wl, probe, nthreads)
-    sample = int(min(wl.batch, max(probe, probe * 2.0 / max(t, 1e-6))))
-    S, X = wl.host_inputs()
-    S, X = S[:sample].copy(), X[:sample].copy()
+    k, t_probe, what = wl.cpu_sample(nthreads, target_s=2.0)
+    vals = []
     for _ in range(args.warmup):
-        oracle.dgesv_batched(S.copy(), X.copy(), nthreads=nthreads)
+        wl.cpu_sample(nthreads, target_s=0.2)
     times = []
     for _ in range(args.steps):
-        s, x = S.copy(), X.copy()
-        t0 = time.perf_counter()
-        oracle.dgesv_batched(s, x, nthreads=nthreads)
-        times.append(time.perf_counter() - t0)
-    tot = sum(times)
-    value = sample * args.steps / tot
+        k2, t, _ = wl.cpu_sample(nthreads, target_s=max(0.5, 2.0 / max(args.steps, 1)))
+        times.append((k2, t))
+    tot_k = sum(k2 for k2, _ in times)
+    tot_t = sum(t for _, t in times)
+    value = tot_k / tot_t
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": wl.describe(), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
-                             "sample": f"each step: {sample} of the {wl.batch} matrices, "
-                                       f"oracle/lu_oracle.c getrf+getrs per matrix, OpenMP over "
+                             "sample": f"each step: a bounded sample of the workload ({what}); "
+                                       f"oracle/lu_oracle.c dgetrf+dgetrs per matrix, OpenMP over "
                                        f"{nthreads} host threads"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -240,14 +491,11 @@ def run_reference(args, wl):
 # --------------------------------------------------------------------------
 # GPU leg
 
-METRIC = "FP64-accurate batched solves/s"
-
 
 def run_ours(args, wl):
     import torch
-    import magma_gb300 as mg
     from magma_gb300 import lib as L
-    from magma_gb300.batched import Queue, ptr_array
+    from magma_gb300.batched import Queue
 
     world, rank, local, pg = dist_setup()
     torch.cuda.set_device(local)
@@ -255,45 +503,20 @@ def run_ours(args, wl):
     lib = L.load()
     stream = torch.cuda.current_stream(dev)
     q = Queue.current(dev)
-
-    S_h, X_h = wl.host_inputs()
-    b, n, r = wl.batch, wl.n, wl.nrhs
     nsteps = args.warmup + args.steps
-    S0 = torch.from_numpy(S_h).to(dev)
-    X0 = torch.from_numpy(X_h).to(dev)
-    # one private copy of the inputs per step
-    Ss = [S0.clone() for _ in range(nsteps)]
-    Xs = [X0.clone() for _ in range(nsteps)]
-    ipiv = torch.empty((b, n), dtype=torch.int32, device=dev)
-    info = torch.empty((b,), dtype=torch.int32, device=dev)
-    dP = ptr_array(ipiv)
-    dAs = [ptr_array(s) for s in Ss]
-    dBs = [ptr_array(x) for x in Xs]
-    fn = lib.magma_dgesv_batched
-
-    def call(i):
-        rc = fn(n, r, C.c_void_p(dAs[i].data_ptr()), n, C.c_void_p(dP.data_ptr()),
-                C.c_void_p(dBs[i].data_ptr()), n, C.c_void_p(info.data_ptr()), b, q.handle)
-        if rc != 0:
-            raise RuntimeError(f"magma_dgesv_batched returned {rc}")
+    c = wl.setup(dev, nsteps, lib, q)
 
     for i in range(args.warmup):
-        call(i)
+        wl.step(c, i)
     torch.cuda.synchronize(dev)
     if args.profile:
-        # profiling mode: only the timed launches, nothing else (for ncu captures)
         for k in range(args.steps):
-            call(args.warmup + k)
+            wl.step(c, args.warmup + k)
         torch.cuda.synchronize(dev)
         return 0
 
-    # peaks for the roofline denominators, measured on this device
-    probe = C.CDLL(str(ROOT / "magma_gb300" / "libmlu_probe.so"))
-    probe.mlu_probe_fp64_tflops.restype = C.c_double
-    probe.mlu_probe_fp64_tflops.argtypes = [C.c_void_p]
-    fp64_peak = probe.mlu_probe_fp64_tflops(C.c_void_p(stream.cuda_stream))
+    peaks = measured_peaks(stream.cuda_stream)
     torch.cuda.synchronize(dev)
-
     clocks = Clocks(local)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
@@ -306,93 +529,60 @@ def run_ours(args, wl):
     start.record(stream)
     for k in range(args.steps):
         ev[k][0].record(stream)
-        call(args.warmup + k)
+        wl.step(c, args.warmup + k)
         ev[k][1].record(stream)
     end.record(stream)
     torch.cuda.synchronize(dev)
     barrier(pg, dev)
     clk = clocks.stop()
-    ms = start.elapsed_time(end)
-    ms = allmax(pg, ms, dev)
-    per_launch_ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in ev)
+    ms = allmax(pg, start.elapsed_time(end), dev)
+    step_ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in ev)
     ms_per_step = ms / args.steps
-    value = world * b / (ms_per_step * 1e-3)
-
-    # correctness of what was timed: the last step against the accuracy criterion
-    A = torch.from_numpy(S_h).to(dev).transpose(1, 2)
-    Xsol = Xs[-1][:, :, :n].transpose(1, 2)
-    Bm = X0[:, :, :n].transpose(1, 2)
-    R = A @ Xsol - Bm
-    eps = float(np.finfo(np.float64).eps)
-    res = (R.abs().sum(2).amax(1) / (A.abs().sum(2).amax(1) * Xsol.abs().sum(2).amax(1) * n * eps))
-    max_res = float(res.max())
-    n_ok = int((res <= 30).sum())
+    acc = wl.accuracy(c, nsteps - 1)
+    n_ok, max_res = acc[0], acc[1]
+    extra = acc[2] if len(acc) > 2 else {}
+    value = world * n_ok / (ms_per_step * 1e-3)
 
     # end to end through the C ABI with pinned host buffers
-    hS = torch.from_numpy(S_h).pin_memory()
-    hX = torch.from_numpy(X_h).pin_memory()
-    hXo = torch.empty_like(hX).pin_memory()
-    hInfo = torch.empty((b,), dtype=torch.int32).pin_memory()
-    dS, dX = Ss[0], Xs[0]
-
-    def e2e_step():
-        dS.copy_(hS, non_blocking=True)
-        dX.copy_(hX, non_blocking=True)
-        call(0)
-        hXo.copy_(dX, non_blocking=True)
-        hInfo.copy_(info, non_blocking=True)
-
+    h2d, d2h = wl.e2e_setup(c)
     for _ in range(max(args.warmup, 1)):
-        e2e_step()
+        wl.e2e_step(c)
     torch.cuda.synchronize(dev)
     barrier(pg, dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        e2e_step()
+        wl.e2e_step(c)
     e1.record(stream)
     torch.cuda.synchronize(dev)
     e2e_ms = allmax(pg, e0.elapsed_time(e1), dev) / args.steps
-    h2d = hS.numel() * 8 + hX.numel() * 8
-    d2h = hXo.numel() * 8 + hInfo.numel() * 4
+
+    fp64 = wl.fp64_path(c, max(2, min(args.steps, 5)), min(args.warmup, 3)) \
+        if hasattr(wl, "fp64_path") else None
 
     if rank != 0:
         return 0
-    flops_launch = wl.flops_per_solve() * b
-    bytes_launch = wl.bytes_per_solve() * b
-    achieved_tf = flops_launch / (per_launch_ms * 1e-3) / 1e12
     cpu = cpu_baseline(wl) if world == 1 else None
-    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
-        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
-        traffic = json.loads(tfile.read_text()).get(wl.name)
+    roof = wl.roofline(step_ms, peaks)
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": wl.dtype,
         "data": "synthetic", "config": wl.describe(),
-        "roofline": {"bound": "fp64", "achieved": achieved_tf, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak if fp64_peak > 0 else None,
-                     "traffic": traffic,
-                     "peak_source": "live FP64 FMA-throughput probe (magma_gb300/probe/peaks.cu)",
-                     "kernel": "small_gesv_kernel<double,32,1>",
-                     "algorithmic_flops_per_launch": flops_launch,
-                     "algorithmic_bytes_per_launch": bytes_launch,
-                     "hbm_achieved_gbs": bytes_launch / (per_launch_ms * 1e-3) / 1e9,
-                     "hbm_peak_gbs": hbm_peak,
-                     "hbm_frac": bytes_launch / (per_launch_ms * 1e-3) / 1e9 / hbm_peak,
-                     "launch_ms": per_launch_ms},
+        "roofline": roof,
         "cpu_baseline": cpu,
-        "e2e": {"value": world * b / (e2e_ms * 1e-3), "unit": "solves/s",
+        "e2e": {"value": world * wl.batch / (e2e_ms * 1e-3), "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "gpu_launches": args.steps,
+        "gpu_launches": (wl.kernels_per_step * args.steps) if wl.kernels_per_step else None,
         "clocks": clk,
-        "accuracy": {"max_scaled_residual": max_res, "solves_within_30": n_ok, "of": b},
+        "accuracy": {"max_scaled_residual": max_res, "solves_within_30": n_ok, "of": wl.batch,
+                     **extra},
+        "peaks_measured": peaks,
     }
+    if fp64 is not None:
+        line["fp64_path"] = fp64
+        line["speedup_vs_fp64_path"] = value / fp64["value"] if fp64["value"] > 0 else None
     print(json.dumps(line), flush=True)
     return 0
 
@@ -400,10 +590,10 @@ def run_ours(args, wl):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="gesv32", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="dsgesv512", choices=sorted(WORKLOADS))
     ap.add_argument("--profile", action="store_true",
                     help="run warm-up and timed launches only (for ncu), print nothing")
     args = ap.parse_args()

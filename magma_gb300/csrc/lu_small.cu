@@ -24,33 +24,40 @@
 
 namespace mlu {
 
-constexpr int SMALL_WARPS = 4;   // matrices per CTA
+constexpr int SMALL_WARPS = 4;   // matrices per CTA (solve kernel)
+constexpr int GESV_WARPS = 8;    // matrices per CTA (factor kernel, lockstep)
 
+// The factor kernel runs its GESV_WARPS warps in lockstep so that the pivot
+// reciprocals of all of them come from one FP64 division sequence issued by
+// warp 0 (one lane per matrix): on this part the FP64 pipe, not latency, is
+// the limit, and a division costs as many FP64 issue slots whether one lane or
+// thirty-two use it.
 template <typename T, int N, int NRHS>
-__global__ void __launch_bounds__(SMALL_WARPS * 32)
+__global__ void __launch_bounds__(GESV_WARPS * 32, 2)
 small_gesv_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T **dB_array,
                   int lddb, int *info_array, int batch)
 {
-    const int lane = threadIdx.x & 31;
-    const int mat = blockIdx.x * SMALL_WARPS + (threadIdx.x >> 5);
-    if (mat >= batch) return;   // uniform per warp
+    __shared__ T s_piv[GESV_WARPS], s_rcp[GESV_WARPS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int mat = blockIdx.x * GESV_WARPS + warp;
+    const bool live = mat < batch;   // dead warps still take part in the barriers
 
-    T *A = dA_array[mat];
+    T *A = live ? dA_array[mat] : nullptr;
     const bool row_valid = lane < n;
 
     T a[N];
 #pragma unroll
     for (int j = 0; j < N; j++)
-        a[j] = (row_valid && j < n) ? A[lane + (size_t)j * ldda] : T(0);
+        a[j] = (live && row_valid && j < n) ? A[lane + (size_t)j * ldda] : T(0);
 
     constexpr int NB = NRHS > 0 ? NRHS : 1;
     T b[NB];
     T *B = nullptr;
     if (NRHS > 0) {
-        B = dB_array[mat];
+        B = live ? dB_array[mat] : nullptr;
 #pragma unroll
         for (int c = 0; c < NB; c++)
-            b[c] = (row_valid && c < nrhs) ? B[lane + (size_t)c * lddb] : T(0);
+            b[c] = (live && row_valid && c < nrhs) ? B[lane + (size_t)c * lddb] : T(0);
     }
 
     unsigned pos = lane;      // position in LAPACK's current row order
@@ -74,7 +81,11 @@ small_gesv_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T *
         const T piv = shfl(v, plane);
         const bool nz = Prec<T>::nonzero(piv);
         if (!nz && info == 0) info = k + 1;
-        const T r = T(1) / piv;
+        if (lane == 0) s_piv[warp] = piv;
+        __syncthreads();
+        if (warp == 0 && lane < GESV_WARPS) s_rcp[lane] = T(1) / s_piv[lane];
+        __syncthreads();
+        const T r = s_rcp[warp];
         if (lane == k) my_ipiv = (int)ppos + 1;
         const bool was_k = (pos == (unsigned)k);
         if (lane == plane) { pos = k; active = false; my_rcp = r; }
@@ -119,7 +130,7 @@ small_gesv_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T *
         }
     }
 
-    if (row_valid) {
+    if (live && row_valid) {
 #pragma unroll
         for (int j = 0; j < N; j++)
             if (j < n) A[pos + (size_t)j * ldda] = a[j];
@@ -130,7 +141,7 @@ small_gesv_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T *
                 if (c < nrhs) B[pos + (size_t)c * lddb] = b[c];
         }
     }
-    if (lane == 0) info_array[mat] = info;
+    if (live && lane == 0) info_array[mat] = info;
 }
 
 // Solve with existing factors, n <= 32.  NoTrans: lane i holds row i of LU.
@@ -248,7 +259,7 @@ template <typename T, int N, int NRHS>
 static void launch_small_gesv(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb,
                               int *info, int batch, cudaStream_t s)
 {
-    small_gesv_kernel<T, N, NRHS><<<mlu_ceildiv(batch, SMALL_WARPS), SMALL_WARPS * 32, 0, s>>>(
+    small_gesv_kernel<T, N, NRHS><<<mlu_ceildiv(batch, GESV_WARPS), GESV_WARPS * 32, 0, s>>>(
         n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch);
 }
 

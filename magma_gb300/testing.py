@@ -36,13 +36,15 @@ def svd_batch_torch(batch: int, n: int, kappas, seed: int, device="cuda"):
     kap = torch.as_tensor(np.asarray(kappas, dtype=np.float64))
     out = torch.empty((batch, n, n), dtype=torch.float64, device=device)
     chunk = 64
+    # QR on the host (LAPACK through torch's CPU build): the same numbers on any
+    # device, and no dependency on the GPU linear-algebra libraries
     for s in range(0, batch, chunk):
         e = min(batch, s + chunk)
-        G1 = torch.randn((e - s, n, n), generator=g, dtype=torch.float64).to(device)
-        G2 = torch.randn((e - s, n, n), generator=g, dtype=torch.float64).to(device)
+        G1 = torch.randn((e - s, n, n), generator=g, dtype=torch.float64)
+        G2 = torch.randn((e - s, n, n), generator=g, dtype=torch.float64)
         U, _ = torch.linalg.qr(G1)
         V, _ = torch.linalg.qr(G2)
-        t = torch.linspace(0.0, 1.0, n, dtype=torch.float64, device=device)
-        sig = torch.exp(-t[None, :] * torch.log(kap[s:e].to(device))[:, None])
-        out[s:e] = (U * sig[:, None, :]) @ V.transpose(1, 2)
+        t = torch.linspace(0.0, 1.0, n, dtype=torch.float64)
+        sig = torch.exp(-t[None, :] * torch.log(kap[s:e])[:, None])
+        out[s:e] = ((U * sig[:, None, :]) @ V.transpose(1, 2)).to(device)
     return out

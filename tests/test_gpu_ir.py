@@ -44,8 +44,8 @@ def _assert_same(gpu, ref, n):
     assert np.array_equal(iters, riters), (iters, riters)
     assert np.array_equal(info, rinfo)
     assert np.array_equal(ipiv[:, :n], ripiv[:, :n])
-    assert np.array_equal(X, rX)
-    assert np.array_equal(S, rS)
+    assert np.array_equal(X, rX, equal_nan=True)     # singular matrices give inf/NaN
+    assert np.array_equal(S, rS, equal_nan=True)
 
 
 @pytest.mark.parametrize("tol", [0.0, 30.0])
