@@ -260,6 +260,26 @@ magma_int_t magma_dsgesv_batched_work(magma_int_t n, magma_int_t nrhs,
                                       void *work, size_t *lwork,
                                       magma_int_t batchCount, magma_queue_t queue);
 
+/* No counterpart in the reference.  The same solve as magma_dsgesv_batched
+ * (same arguments, ITER codes and FP64 re-solve) for callers that cannot
+ * allocate device memory -- a process whose device memory is reserved by
+ * another allocator, code where allocation calls are not allowed, or a
+ * foreign-language binding with no way to own a device buffer.  It allocates
+ * nothing: its scratch is a 32 MiB array compiled into the library, present on
+ * every GPU that loads it until the process exits.  Returns
+ * MAGMA_ERR_NOT_SUPPORTED, with a message, when the batch needs more scratch
+ * than that (workspace size: magma_dsgesv_batched_work with work == NULL).
+ * The first call on each device looks up the array's address and should come
+ * before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU race, so issue them in order on one stream. */
+magma_int_t magma_dsgesv_batched_noalloc(magma_int_t n, magma_int_t nrhs,
+                                         double **dA_array, magma_int_t ldda,
+                                         magma_int_t **dipiv_array,
+                                         double **dB_array, magma_int_t lddb,
+                                         double **dX_array, magma_int_t lddx,
+                                         magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                         magma_int_t batchCount, magma_queue_t queue);
+
 #ifdef __cplusplus
 }
 #endif

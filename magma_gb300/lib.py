@@ -51,6 +51,8 @@ for _p in "ds":
     _PROTOS[f"magma_{_p}gesv_batched_small"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_dsgesv_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr, c_int,
                                    c_ptr, c_ptr, c_int, c_ptr], c_int)
+_PROTOS["magma_dsgesv_batched_noalloc"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr,
+                                           c_int, c_ptr, c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_dsgesv_batched_work"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr,
                                         c_int, c_ptr, c_ptr, c_int, C.c_double, c_int, c_ptr,
                                         C.POINTER(C.c_size_t), c_int, c_ptr], c_int)
