@@ -332,7 +332,262 @@ class Dsgesv512:
         return k, statistics.median(ts), f"{k} of the {self.batch} matrices (FP64 dgetrf+dgetrs)"
 
 
-WORKLOADS = {"dsgesv512": Dsgesv512, "gesv32": Gesv32}
+class GesvVbatched:
+    """Variable-size FP64 factor+solve (magma_dgesv_vbatched_max_nocheck_work,
+    one persistent launch after a device-side size sort), CUDA-graph captured."""
+    name = "vbatched4096"
+    batch = 4096
+    seed = 20240602
+    dtype = "f64"
+
+    def describe(self):
+        return {"workload": "magma_dgesv_vbatched: 4096 FP64 matrices, n uniform in [8,256], "
+                            "nrhs uniform in [1,16], entries uniform(-1,1); one persistent "
+                            "size-sorted launch replayed from a CUDA graph",
+                "batch": self.batch, "n": "U[8,256]", "nrhs": "U[1,16]", "precision": "fp64",
+                "l2": "inputs larger than L2: each step owns a private copy (~0.7 GB)"}
+
+    def sizes(self):
+        rng = np.random.default_rng(self.seed)
+        ns = rng.integers(8, 257, self.batch)
+        rs = rng.integers(1, 17, self.batch)
+        return [int(x) for x in ns], [int(x) for x in rs]
+
+    def host_inputs(self):
+        ns, rs = self.sizes()
+        rng = np.random.default_rng(self.seed + 1)
+        As = [rng.uniform(-1, 1, (n, n)) for n in ns]     # storage (ncols, ld)
+        Bs = [rng.uniform(-1, 1, (r, n)) for n, r in zip(ns, rs)]
+        return ns, rs, As, Bs
+
+    def flops_total(self):
+        ns, rs = self.sizes()
+        return sum(flops_getrf(n, n) + flops_getrs(n, r) for n, r in zip(ns, rs))
+
+    def setup(self, dev, nsteps, lib, q):
+        import torch
+        from magma_gb300.batched import VBatch, Queue
+        ns, rs, As, Bs = self.host_inputs()
+        c = {"ns": ns, "rs": rs, "As": As, "Bs": Bs, "lib": lib}
+        A0 = VBatch([a.shape for a in As], ns, torch.float64, dev).load(As)
+        B0 = VBatch([b.shape for b in Bs], ns, torch.float64, dev).load(Bs)
+        c["A0"], c["B0"] = A0, B0
+        offs = np.concatenate([[0], np.cumsum(ns)[:-1]])
+        c["ipiv"] = torch.zeros((sum(ns),), dtype=torch.int32, device=dev)
+        c["dP"] = c["ipiv"].data_ptr() + torch.tensor(offs, dtype=torch.int64, device=dev) * 4
+        c["info"] = torch.empty((self.batch,), dtype=torch.int32, device=dev)
+        lw = C.c_int(-1)
+        lib.magma_dgesv_vbatched_max_nocheck_work(None, None, 256, 16, None, None, None, None,
+                                                  None, None, None, C.byref(lw), self.batch, None)
+        c["lwork"] = lw
+        c["work"] = torch.empty((lw.value,), dtype=torch.uint8, device=dev)
+        # one private copy per step, each with its own captured graph
+        c["A"], c["B"], c["graphs"] = [], [], []
+        stream = torch.cuda.Stream(dev)
+        c["gstream"] = stream
+        c["gq"] = Queue(dev.index, stream.cuda_stream)
+        for i in range(nsteps):
+            A = VBatch(A0.shapes, ns, torch.float64, dev)
+            B = VBatch(B0.shapes, ns, torch.float64, dev)
+            A.buf.copy_(A0.buf)
+            B.buf.copy_(B0.buf)
+            c["A"].append(A)
+            c["B"].append(B)
+        torch.cuda.synchronize(dev)
+        for i in range(nsteps):
+            A, B = c["A"][i], c["B"][i]
+            with torch.cuda.stream(stream):
+                self._call(c, A, B, c["gq"])          # eager once (kernel attributes)
+                stream.synchronize()
+                A.buf.copy_(A0.buf)
+                B.buf.copy_(B0.buf)
+                stream.synchronize()
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=stream):
+                    self._call(c, A, B, c["gq"])
+            c["graphs"].append(g)
+        torch.cuda.synchronize(dev)
+        return c
+
+    def _call(self, c, A, B, q):
+        rc = c["lib"].magma_dgesv_vbatched_max_nocheck_work(
+            vp(A.ncols), vp(B.ncols), 256, 16, vp(A.ptrs), vp(A.ld), vp(c["dP"]), vp(B.ptrs),
+            vp(B.ld), vp(c["info"]), vp(c["work"]), C.byref(c["lwork"]), self.batch, q.handle)
+        if rc != 0:
+            raise RuntimeError(f"magma_dgesv_vbatched_max_nocheck_work returned {rc}")
+
+    def step(self, c, i):
+        c["graphs"][i].replay()
+
+    kernels_per_step = 2
+    dominant = "mlu::vb_lu_kernel<double> (persistent)"
+
+    def e2e_setup(self, c):
+        import torch
+        c["hA"] = c["A0"].buf.cpu().pin_memory()
+        c["hB"] = c["B0"].buf.cpu().pin_memory()
+        c["hX"] = torch.empty_like(c["hB"]).pin_memory()
+        c["hInfo"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
+        return c["hA"].numel() * 8 + c["hB"].numel() * 8, c["hX"].numel() * 8 + self.batch * 4
+
+    def e2e_step(self, c):
+        c["A"][0].buf.copy_(c["hA"], non_blocking=True)
+        c["B"][0].buf.copy_(c["hB"], non_blocking=True)
+        c["graphs"][0].replay()
+        c["hX"].copy_(c["B"][0].buf, non_blocking=True)
+        c["hInfo"].copy_(c["info"], non_blocking=True)
+
+    def accuracy(self, c, last):
+        import torch
+        ns, rs, As, Bs = c["ns"], c["rs"], c["As"], c["Bs"]
+        B = c["B"][last]
+        worst, ok = 0.0, 0
+        for k in range(self.batch):
+            A = torch.from_numpy(As[k].T.copy())
+            X = B.view(k).cpu().T
+            Bm = torch.from_numpy(Bs[k].T.copy())
+            r = float(scaled_residuals(A[None], X[None], Bm[None])[0])
+            worst = max(worst, r)
+            ok += r <= 30
+        return ok, worst
+
+    def roofline(self, step_ms, peaks):
+        flops = self.flops_total()
+        ach = flops / (step_ms * 1e-3) / 1e12
+        return {"bound": "fp64", "achieved": ach, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["fp64_tflops"], "traffic": _traffic(self.name),
+                "peak_source": "FP64 FMA-throughput probe run inside bench.py",
+                "kernel": self.dominant, "launch_ms": step_ms,
+                "algorithmic_flops_per_launch": flops}
+
+    def cpu_sample(self, nthreads, target_s):
+        import oracle
+        ns, rs, As, Bs = self.host_inputs()
+
+        def run(k):
+            a = [x.copy() for x in As[:k]]
+            b = [x.copy() for x in Bs[:k]]
+            t0 = time.perf_counter()
+            oracle.dgesv_vbatched(ns[:k], rs[:k], a, b, nthreads=nthreads)
+            return time.perf_counter() - t0
+        k = 256
+        t = run(k)
+        k = int(min(self.batch, max(k, k * target_s / max(t, 1e-6))))
+        ts = [run(k) for _ in range(3)]
+        return k, statistics.median(ts), f"the first {k} of the {self.batch} matrices"
+
+
+class Adjoint2048:
+    """Differentiable solve: forward magma_dgesv_batched + backward
+    magma_dgesv_adjoint_batched through magma_gb300.autograd.solve."""
+    name = "adjoint2048"
+    batch, n, nrhs = 2048, 64, 4
+    seed = 20240604
+    dtype = "f64"
+
+    def describe(self):
+        return {"workload": "autograd solve x = A^{-1} b, forward + backward: 2048 FP64 matrices "
+                            "n=64, A = 4I + uniform(-1,1), nrhs=4, upstream gradient N(0,1)",
+                "batch": self.batch, "n": self.n, "nrhs": self.nrhs, "precision": "fp64",
+                "l2": "each step owns its inputs (34 MB) and writes gA (34 MB)"}
+
+    def setup(self, dev, nsteps, lib, q):
+        import torch
+        g = torch.Generator(device="cpu").manual_seed(self.seed)
+        b, n, r = self.batch, self.n, self.nrhs
+        A = 4.0 * torch.eye(n, dtype=torch.float64) + (torch.rand((b, n, n), generator=g,
+                                                                  dtype=torch.float64) * 2 - 1)
+        B = torch.rand((b, n, r), generator=g, dtype=torch.float64) * 2 - 1
+        gX = torch.randn((b, n, r), generator=g, dtype=torch.float64)
+        c = {"A0": A.to(dev), "B0": B.to(dev), "gX": gX.to(dev)}
+        c["hA"], c["hB"], c["hgX"] = A.pin_memory(), B.pin_memory(), gX.pin_memory()
+        c["As"] = [c["A0"].clone().requires_grad_(True) for _ in range(nsteps)]
+        c["Bs"] = [c["B0"].clone().requires_grad_(True) for _ in range(nsteps)]
+        return c
+
+    def step(self, c, i):
+        from magma_gb300.autograd import solve
+        A, B = c["As"][i], c["Bs"][i]
+        A.grad = None
+        B.grad = None
+        X = solve(A, B)
+        X.backward(c["gX"])
+        c["last_X"] = X
+
+    kernels_per_step = None
+    dominant = "forward small-n LU (blocked path, n=64) + adjoint"
+
+    def e2e_setup(self, c):
+        import torch
+        c["hgA"] = torch.empty((self.batch, self.n, self.n), dtype=torch.float64).pin_memory()
+        c["hgB"] = torch.empty((self.batch, self.n, self.nrhs), dtype=torch.float64).pin_memory()
+        c["dA"] = torch.empty_like(c["A0"])
+        c["dB"] = torch.empty_like(c["B0"])
+        c["dg"] = torch.empty_like(c["gX"])
+        h2d = (c["hA"].numel() + c["hB"].numel() + c["hgX"].numel()) * 8
+        d2h = (c["hgA"].numel() + c["hgB"].numel()) * 8
+        return h2d, d2h
+
+    def e2e_step(self, c):
+        from magma_gb300.autograd import solve
+        c["dA"].copy_(c["hA"], non_blocking=True)
+        c["dB"].copy_(c["hB"], non_blocking=True)
+        c["dg"].copy_(c["hgX"], non_blocking=True)
+        A = c["dA"].detach().requires_grad_(True)
+        B = c["dB"].detach().requires_grad_(True)
+        solve(A, B).backward(c["dg"])
+        c["hgA"].copy_(A.grad, non_blocking=True)
+        c["hgB"].copy_(B.grad, non_blocking=True)
+
+    def accuracy(self, c, last):
+        import torch
+        A = c["A0"].clone().requires_grad_(True)
+        B = c["B0"].clone().requires_grad_(True)
+        X = torch.linalg.solve(A, B)
+        X.backward(c["gX"])
+        Ag = c["As"][last].grad
+        rel = float((Ag - A.grad).abs().max() / A.grad.abs().max())
+        res = scaled_residuals(c["A0"], c["last_X"].detach(), c["B0"])
+        return int((res <= 30).sum()), float(res.max()), {"grad_rel_err_vs_torch_fp64": rel}
+
+    def roofline(self, step_ms, peaks):
+        b, n, r = self.batch, self.n, self.nrhs
+        flops = b * (flops_getrf(n, n) + flops_getrs(n, r) + flops_getrs(n, r) + 2.0 * n * n * r)
+        ach = flops / (step_ms * 1e-3) / 1e12
+        return {"bound": "fp64", "achieved": ach, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["fp64_tflops"], "traffic": None,
+                "peak_source": "FP64 FMA-throughput probe run inside bench.py",
+                "kernel": self.dominant, "launch_ms": step_ms,
+                "algorithmic_flops_per_launch": flops}
+
+    def cpu_sample(self, nthreads, target_s):
+        import oracle
+        import torch
+        g = torch.Generator(device="cpu").manual_seed(self.seed)
+        b, n, r = self.batch, self.n, self.nrhs
+        A = 4.0 * torch.eye(n, dtype=torch.float64) + (torch.rand((b, n, n), generator=g,
+                                                                  dtype=torch.float64) * 2 - 1)
+        B = torch.rand((b, n, r), generator=g, dtype=torch.float64) * 2 - 1
+        gX = torch.randn((b, n, r), generator=g, dtype=torch.float64)
+        S0 = A.transpose(1, 2).contiguous().numpy()
+        X0 = B.transpose(1, 2).contiguous().numpy()
+        G0 = gX.transpose(1, 2).contiguous().numpy()
+
+        def run(k):
+            S, X, G = S0[:k].copy(), X0[:k].copy(), G0[:k].copy()
+            t0 = time.perf_counter()
+            ipiv, _ = oracle.dgesv_batched(S, X, nthreads=nthreads)
+            oracle.gesv_adjoint_batched(S, ipiv, X, G, nthreads=nthreads)
+            return time.perf_counter() - t0
+        k = 256
+        t = run(k)
+        k = int(min(b, max(k, k * target_s / max(t, 1e-6))))
+        ts = [run(k) for _ in range(3)]
+        return k, statistics.median(ts), f"{k} of the {b} forward+backward solves"
+
+
+WORKLOADS = {"dsgesv512": Dsgesv512, "gesv32": Gesv32, "vbatched4096": GesvVbatched,
+             "adjoint2048": Adjoint2048}
 
 
 def _traffic(name):

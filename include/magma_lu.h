@@ -218,6 +218,141 @@ magma_int_t magma_sgesv_batched_small(magma_int_t n, magma_int_t nrhs,
                                       magma_int_t batchCount, magma_queue_t queue);
 
 /* ------------------------------------------------------------------------ */
+/* Batched LU, variable size -- include/magma_zvbatched.h                   */
+/* m, n, nrhs, ldda, lddb are device arrays of batchCount ints.             */
+
+/* include/magma_zvbatched.h:57, src/zgetrf_vbatched.cpp:341-398.  Checks the
+ * sizes on the device and reads back their maxima (one synchronisation of the
+ * queue's stream, as MAGMA does); returns 0 or -1 (some m<0), -2 (some n<0),
+ * -4 (some ldda<max(1,m)).  Grows the queue's workspace when needed. */
+magma_int_t magma_dgetrf_vbatched(magma_int_t *m, magma_int_t *n,
+                                  double **dA_array, magma_int_t *ldda,
+                                  magma_int_t **ipiv_array, magma_int_t *info_array,
+                                  magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetrf_vbatched(magma_int_t *m, magma_int_t *n,
+                                  float **dA_array, magma_int_t *ldda,
+                                  magma_int_t **ipiv_array, magma_int_t *info_array,
+                                  magma_int_t batchCount, magma_queue_t queue);
+
+/* include/magma_zvbatched.h:73, src/zgetrf_vbatched.cpp:224-282.  The caller
+ * provides the maxima and a workspace (*lwork < 0: *lwork receives the bytes
+ * needed and nothing else happens); no checks, no allocation, no host
+ * synchronisation -- capturable in a CUDA graph.  max_minmn and max_mxn are
+ * accepted for ABI compatibility and unused.  Returns -12 if *lwork is too
+ * small. */
+magma_int_t magma_dgetrf_vbatched_max_nocheck_work(magma_int_t *m, magma_int_t *n,
+                                                   magma_int_t max_m, magma_int_t max_n,
+                                                   magma_int_t max_minmn, magma_int_t max_mxn,
+                                                   double **dA_array, magma_int_t *ldda,
+                                                   magma_int_t **dipiv_array,
+                                                   magma_int_t *info_array,
+                                                   void *work, magma_int_t *lwork,
+                                                   magma_int_t batchCount, magma_queue_t queue);
+
+/* No counterpart in the reference (MAGMA has no variable-size solve).
+ * Arguments as magma_dgetrs_batched with per-matrix n, nrhs, ldda, lddb.
+ * Returns 0 or -1 (trans), -2 (some n<0), -3 (some nrhs<0), -5 (ldda), -8 (lddb).
+ * One synchronisation to read the maxima. */
+magma_int_t magma_dgetrs_vbatched(magma_trans_t trans, magma_int_t *n, magma_int_t *nrhs,
+                                  double **dA_array, magma_int_t *ldda,
+                                  magma_int_t **dipiv_array,
+                                  double **dB_array, magma_int_t *lddb,
+                                  magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetrs_vbatched(magma_trans_t trans, magma_int_t *n, magma_int_t *nrhs,
+                                  float **dA_array, magma_int_t *ldda,
+                                  magma_int_t **dipiv_array,
+                                  float **dB_array, magma_int_t *lddb,
+                                  magma_int_t batchCount, magma_queue_t queue);
+
+/* No counterpart in the reference.  Factor and solve, variable sizes, in one
+ * persistent launch.  Returns 0 or -1 (some n<0), -2 (some nrhs<0), -4 (ldda),
+ * -7 (lddb).  One synchronisation to check and read the maxima. */
+magma_int_t magma_dgesv_vbatched(magma_int_t *n, magma_int_t *nrhs,
+                                 double **dA_array, magma_int_t *ldda,
+                                 magma_int_t **dipiv_array,
+                                 double **dB_array, magma_int_t *lddb,
+                                 magma_int_t *dinfo_array,
+                                 magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgesv_vbatched(magma_int_t *n, magma_int_t *nrhs,
+                                 float **dA_array, magma_int_t *ldda,
+                                 magma_int_t **dipiv_array,
+                                 float **dB_array, magma_int_t *lddb,
+                                 magma_int_t *dinfo_array,
+                                 magma_int_t batchCount, magma_queue_t queue);
+
+/* No counterpart in the reference: magma_dgesv_vbatched with caller-provided
+ * maxima and workspace, in the style of magma_dgetrf_vbatched_max_nocheck_work;
+ * no checks, allocation or synchronisation -- capturable in a CUDA graph. */
+magma_int_t magma_dgesv_vbatched_max_nocheck_work(magma_int_t *n, magma_int_t *nrhs,
+                                                  magma_int_t max_n, magma_int_t max_nrhs,
+                                                  double **dA_array, magma_int_t *ldda,
+                                                  magma_int_t **dipiv_array,
+                                                  double **dB_array, magma_int_t *lddb,
+                                                  magma_int_t *dinfo_array,
+                                                  void *work, magma_int_t *lwork,
+                                                  magma_int_t batchCount, magma_queue_t queue);
+
+/* ------------------------------------------------------------------------ */
+/* Adjoint of the batched solve.  No counterpart in the reference (MAGMA has
+ * no autograd).  Given the forward factors (magma_?getrf_batched or
+ * magma_?gesv_batched output: LU in dLU_array, pivots in dipiv_array), the
+ * solutions X and the upstream gradients G = dL/dX (overwritten by
+ * dL/dB = A^{-T} G), writes dL/dA = -(A^{-T} G) X^T to dGA_array.
+ * Returns 0 or -i for an illegal argument i (n, nrhs, ldda = 4, lddx = 7,
+ * lddg = 9, lddga = 11). */
+magma_int_t magma_dgesv_adjoint_batched(magma_int_t n, magma_int_t nrhs,
+                                        double **dLU_array, magma_int_t ldda,
+                                        magma_int_t **dipiv_array,
+                                        double **dX_array, magma_int_t lddx,
+                                        double **dG_array, magma_int_t lddg,
+                                        double **dGA_array, magma_int_t lddga,
+                                        magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgesv_adjoint_batched(magma_int_t n, magma_int_t nrhs,
+                                        float **dLU_array, magma_int_t ldda,
+                                        magma_int_t **dipiv_array,
+                                        float **dX_array, magma_int_t lddx,
+                                        float **dG_array, magma_int_t lddg,
+                                        float **dGA_array, magma_int_t lddga,
+                                        magma_int_t batchCount, magma_queue_t queue);
+
+/* GA_k = -G_k X_k^T (n x n, rank nrhs) for every k: the outer-product half of
+ * the adjoint, in the naming style of magmablas_zger_batched
+ * (include/magma_zbatched.h).  Returns 0 or -i (n, nrhs, lddg = 4, lddx = 6,
+ * lddga = 8). */
+magma_int_t magmablas_dger_neg_batched(magma_int_t n, magma_int_t nrhs,
+                                       double **dG_array, magma_int_t lddg,
+                                       double **dX_array, magma_int_t lddx,
+                                       double **dGA_array, magma_int_t lddga,
+                                       magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magmablas_sger_neg_batched(magma_int_t n, magma_int_t nrhs,
+                                       float **dG_array, magma_int_t lddg,
+                                       float **dX_array, magma_int_t lddx,
+                                       float **dGA_array, magma_int_t lddga,
+                                       magma_int_t batchCount, magma_queue_t queue);
+
+/* ------------------------------------------------------------------------ */
+/* FP32 factorisation with tensor-core trailing updates.  The batched form of
+ * the reference's half-precision factorisation (magma_xhsgetrf_gpu,
+ * src/xhsgetrf_gpu.cpp:212; Magma_PREC_SHT, include/magma_types.h:861): the
+ * matrix stays FP32, panels, interchanges and TRSM run in FP32, and every
+ * trailing update of at least 128 x 128 runs on the tensor cores with FP16
+ * (precision = 905, Magma_PREC_SHT) or BF16 (precision = 930, no counterpart
+ * in the reference) operands and FP32 accumulation.  work == NULL: *lwork
+ * receives the workspace bytes.  Returns 0, -i for an illegal argument
+ * (precision = 1, m = 2, n = 3, ldda = 5) or -9 if *lwork is too small. */
+#define Magma_PREC_SHT 905
+#define Magma_PREC_SBT 930
+magma_int_t magma_sgetrf_batched_tc(magma_int_t precision, magma_int_t m, magma_int_t n,
+                                    float **dA_array, magma_int_t ldda,
+                                    magma_int_t **ipiv_array, magma_int_t *info_array,
+                                    void *work, size_t *lwork,
+                                    magma_int_t batchCount, magma_queue_t queue);
+/* Error flag left by the last magma_sgetrf_batched_tc in `work` (0: no tensor
+ * pipeline wait timed out); synchronises the queue. */
+magma_int_t magma_sgetrf_batched_tc_status(magma_int_t m, magma_int_t n, void *work,
+                                           magma_int_t batchCount, magma_queue_t queue);
+
+/* ------------------------------------------------------------------------ */
 /* Batched mixed-precision iterative refinement.  MAGMA refines one matrix
  * at a time (magma_dsgesv_gpu, src/zcgesv_gpu.cpp:144-366, declared in
  * include/magma_zc.h); these apply the same algorithm, arguments and ITER
@@ -279,6 +414,26 @@ magma_int_t magma_dsgesv_batched_noalloc(magma_int_t n, magma_int_t nrhs,
                                          double **dX_array, magma_int_t lddx,
                                          magma_int_t *dinfo_array, magma_int_t *diter_array,
                                          magma_int_t batchCount, magma_queue_t queue);
+
+/* No counterpart in the reference: magma_dsgesv_batched_work with the
+ * factorisation precision as first argument -- 900 (Magma_PREC_SS: FP32
+ * factorisation, identical to magma_dsgesv_batched_work), 905
+ * (Magma_PREC_SHT: FP32 storage, trailing updates on the tensor cores with
+ * FP16 operands, the matrix first scaled by powers of two per row and column so
+ * that FP16 cannot overflow) or 930 (Magma_PREC_SBT: BF16 operands, no
+ * scaling).  The half-precision forms converge for moderately conditioned
+ * matrices (kappa * unit roundoff well below 1) and otherwise end with the
+ * FP64 re-solve.  Error codes: -1 precision, then those of
+ * magma_dsgesv_batched_work shifted by one. */
+magma_int_t magma_dxgesv_batched_work(magma_int_t precision, magma_int_t n, magma_int_t nrhs,
+                                      double **dA_array, magma_int_t ldda,
+                                      magma_int_t **dipiv_array,
+                                      double **dB_array, magma_int_t lddb,
+                                      double **dX_array, magma_int_t lddx,
+                                      magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                      magma_int_t itermax, double tol, magma_int_t fallback,
+                                      void *work, size_t *lwork,
+                                      magma_int_t batchCount, magma_queue_t queue);
 
 #ifdef __cplusplus
 }

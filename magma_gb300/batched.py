@@ -164,11 +164,14 @@ def gesv_batched(S: torch.Tensor, B: torch.Tensor, ipiv: torch.Tensor | None = N
     return ipiv, info
 
 
+PRECISIONS = {"fp32": 900, "fp16": 905, "bf16": 930}
+
+
 def dsgesv_batched(S: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = None,
                    itermax: int = 30, tol: float = 0.0, fallback: bool = True,
                    ipiv: torch.Tensor | None = None, info: torch.Tensor | None = None,
                    iters: torch.Tensor | None = None, work: torch.Tensor | None = None,
-                   queue: Queue | None = None):
+                   queue: Queue | None = None, precision: str = "fp32"):
     """Batched FP32-factor / FP64-refinement solve (magma_dsgesv_batched_work).
 
     S and B are FP64 column-major storage and are left unchanged unless a
@@ -188,23 +191,83 @@ def dsgesv_batched(S: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = No
     iters = torch.empty((b,), dtype=torch.int32, device=S.device) if iters is None else iters
     q = queue or Queue.current(S.device)
     lib = _L.load()
-    need = dsgesv_workspace_bytes(n, nrhs, b)
+    prec = PRECISIONS[precision]
+    need = dsgesv_workspace_bytes(n, nrhs, b, precision)
     if work is None or work.numel() < need:
         work = torch.empty((max(need, 1),), dtype=torch.uint8, device=S.device)
     lw = C.c_size_t(work.numel())
     dA, dP, dB, dX = ptr_array(S), ptr_array(ipiv), ptr_array(B), ptr_array(X)
-    rc = lib.magma_dsgesv_batched_work(n, nrhs, _vp(dA), ld, _vp(dP), _vp(dB), ldb, _vp(dX),
+    rc = lib.magma_dxgesv_batched_work(prec, n, nrhs, _vp(dA), ld, _vp(dP), _vp(dB), ldb, _vp(dX),
                                        X.shape[2], _vp(info), _vp(iters), itermax, float(tol),
                                        1 if fallback else 0, _vp(work), C.byref(lw), b, q.handle)
-    _check(rc, "magma_dsgesv_batched_work")
+    _check(rc, "magma_dxgesv_batched_work")
     return X, ipiv, info, iters
 
 
-def dsgesv_workspace_bytes(n: int, nrhs: int, batch: int) -> int:
+def dsgesv_workspace_bytes(n: int, nrhs: int, batch: int, precision: str = "fp32") -> int:
     lib = _L.load()
     lw = C.c_size_t(0)
-    rc = lib.magma_dsgesv_batched_work(n, nrhs, None, max(n, 1), None, None, max(n, 1), None,
-                                       max(n, 1), None, None, 30, 0.0, 0, None, C.byref(lw),
-                                       batch, None)
+    rc = lib.magma_dxgesv_batched_work(PRECISIONS[precision], n, nrhs, None, max(n, 1), None,
+                                       None, max(n, 1), None, max(n, 1), None, None, 30, 0.0, 0,
+                                       None, C.byref(lw), batch, None)
     _check(rc, "magma_dsgesv_batched_work(query)")
     return int(lw.value)
+
+
+class VBatch:
+    """A variable-size batch packed into one device buffer.
+
+    mats: list of column-major storage tensors, matrix k of shape (ncols_k, ld_k)
+    (that is, A_k^T in memory order).  The packed buffer holds them back to back
+    (each start aligned to 64 bytes); `ptrs`, `ld`, `ncols` and `nrows` are the
+    device arrays MAGMA's vbatched routines take."""
+
+    def __init__(self, shapes, nrows, dtype, device):
+        self.shapes = [tuple(s) for s in shapes]
+        self.nrows = list(nrows)
+        elsz = torch.empty((), dtype=dtype).element_size()
+        align = 64 // elsz
+        offs, o = [], 0
+        for (nc, ld) in self.shapes:
+            offs.append(o)
+            o += ((nc * ld + align - 1) // align) * align
+        self.offsets = offs
+        self.buf = torch.zeros((max(o, 1),), dtype=dtype, device=device)
+        base = self.buf.data_ptr()
+        self.ptrs = torch.tensor([base + x * elsz for x in offs], dtype=torch.int64, device=device)
+        self.ld = torch.tensor([ld for (_, ld) in self.shapes], dtype=torch.int32, device=device)
+        self.ncols = torch.tensor([nc for (nc, _) in self.shapes], dtype=torch.int32, device=device)
+        self.rows = torch.tensor(self.nrows, dtype=torch.int32, device=device)
+
+    def view(self, k):
+        nc, ld = self.shapes[k]
+        o = self.offsets[k]
+        return self.buf[o:o + nc * ld].view(nc, ld)
+
+    def load(self, mats):
+        for k, m in enumerate(mats):
+            self.view(k).copy_(torch.as_tensor(m))
+        return self
+
+
+def gesv_vbatched(A: "VBatch", B: "VBatch", queue: Queue | None = None):
+    """In-place factor and solve of a variable-size batch (magma_?gesv_vbatched).
+    Returns (ipiv buffer, per-matrix ipiv offsets, info)."""
+    b = len(A.shapes)
+    lib = _L.load()
+    p = _prefix(A.buf)
+    n = A.ncols
+    nrhs = B.ncols
+    tot = sum(max(s[0], 1) for s in A.shapes)
+    ipiv = torch.zeros((max(tot, 1),), dtype=torch.int32, device=A.buf.device)
+    offs, o = [], 0
+    for (nc, _) in A.shapes:
+        offs.append(o)
+        o += max(nc, 1)
+    dP = ipiv.data_ptr() + torch.tensor(offs, dtype=torch.int64, device=A.buf.device) * 4
+    info = torch.empty((b,), dtype=torch.int32, device=A.buf.device)
+    q = queue or Queue.current(A.buf.device)
+    rc = getattr(lib, f"magma_{p}gesv_vbatched")(_vp(n), _vp(nrhs), _vp(A.ptrs), _vp(A.ld), _vp(dP),
+                                                 _vp(B.ptrs), _vp(B.ld), _vp(info), b, q.handle)
+    _check(rc, f"magma_{p}gesv_vbatched")
+    return ipiv, offs, info

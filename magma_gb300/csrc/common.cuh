@@ -98,6 +98,27 @@ __device__ __forceinline__ T shfl(T v, int src) { return __shfl_sync(FULL, v, sr
         }                                                                               \
     } while (0)
 
+// Lets `kernel` use as much dynamic shared memory as the device allows next to
+// its static shared memory.  Returns that amount in bytes.  Any error of the
+// attribute calls is consumed here so that it cannot surface as a launch error.
+template <typename K>
+static inline size_t mlu_allow_dynamic_smem(K kernel)
+{
+    cudaFuncAttributes fa;
+    int dev = 0, optin = 0;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 48 * 1024;
+    }
+    const int dyn = optin - (int)fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) {
+        cudaGetLastError();
+        return 48 * 1024 - fa.sharedSizeBytes;
+    }
+    return (size_t)dyn;
+}
+
 static inline magma_int_t mlu_max(magma_int_t a, magma_int_t b) { return a > b ? a : b; }
 static inline magma_int_t mlu_min(magma_int_t a, magma_int_t b) { return a < b ? a : b; }
 static inline magma_int_t mlu_ceildiv(magma_int_t a, magma_int_t b) { return (a + b - 1) / b; }

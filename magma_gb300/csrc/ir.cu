@@ -4,7 +4,9 @@
 // (magma_dsgesv_gpu, src/zcgesv_gpu.cpp:144-366; magma_dhgesv_iteref_gpu,
 // src/dxgesv_gmres_gpu.cpp:1122).  This file applies the same algorithm to a
 // whole batch on the device, per matrix:
-//   anrm = ||A||_inf, cte = anrm * eps * sqrt(n)           (zcgesv_gpu.cpp:208-209)
+//   anrm = ||A||_inf, cte = anrm * eps * sqrt(n)           (zcgesv_gpu.cpp:208-209);
+//     here anrm is the infinity norm of float(A) with FP32 row sums, which keeps
+//     the conversion pass off the FP64 pipe (the tolerance changes by ~n*2^-24)
 //   As = float(A) (overflow -> iter = -2), LU of As in FP32 (info > 0 -> iter = -3)
 //   X = 0, R = B; repeat: X += float-solve(R); R = B - A X in FP64;
 //   converged when, for every right-hand side c, ||R_c||_inf <= ||X_c||_inf * cte
@@ -22,6 +24,7 @@
 // the FP64 residual, the oracle's order in the FP32 factor and solves), so the
 // CPU oracle reproduces iterates and iteration counts exactly.
 #include "common.cuh"
+#include "convert.cuh"
 #include "solve_core.cuh"
 
 namespace mlu {
@@ -37,6 +40,13 @@ extern "C" magma_int_t magma_sgetrf_batched(magma_int_t m, magma_int_t n, float 
                                             magma_int_t ldda, magma_int_t **ipiv_array,
                                             magma_int_t *info_array, magma_int_t batchCount,
                                             magma_queue_t queue);
+extern "C" magma_int_t magma_sgetrf_batched_tc(magma_int_t precision, magma_int_t m, magma_int_t n,
+                                               float **dA_array, magma_int_t ldda,
+                                               magma_int_t **ipiv_array, magma_int_t *info_array,
+                                               void *work, size_t *lwork, magma_int_t batchCount,
+                                               magma_queue_t queue);
+extern "C" magma_int_t magma_sgetrf_batched_tc_status(magma_int_t m, magma_int_t n, void *work,
+                                                      magma_int_t batchCount, magma_queue_t queue);
 extern "C" magma_int_t magma_dgesv_batched(magma_int_t n, magma_int_t nrhs, double **dA_array,
                                            magma_int_t ldda, magma_int_t **dipiv_array,
                                            double **dB_array, magma_int_t lddb,
@@ -73,11 +83,23 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, doub
     if ((threadIdx.x & 31) == 0) atomicMax(addr, ((unsigned long long)hi << 32) | lo);
 }
 
-// As = float(A), ||A||_inf, R = B, X = 0.
+// 2^-(e) with e the exponent that puts x * 2^-e in [0.5, 1) (1 for x == 0):
+// an exact power-of-two scale factor.
+__device__ __forceinline__ double pow2_scale(double x)
+{
+    if (!(x > 0.0) || isinf(x)) return 1.0;
+    const int e = ilogb(x) + 1;
+    return ldexp(1.0, -e);
+}
+
+// As = float(A), ||A||_inf, R = B, X = 0.  With rowscale != nullptr (FP16
+// factorisation) the kernel instead records a power-of-two row scale
+// 2^-e_i with max_j |a_ij| 2^-e_i in [0.5, 1) and leaves As to
+// ir_colscale_kernel.
 __global__ void __launch_bounds__(IR_ROWS)
 ir_init_kernel(int n, int nrhs, double **dA_array, int ldda, float **dAs_array, int ldas,
                double **dB_array, int lddb, double **dX_array, int lddx, double *R,
-               unsigned long long *stats, int *iter)
+               unsigned long long *stats, int *iter, double *rowscale)
 {
     const int mat = blockIdx.y;
     const int i = blockIdx.x * IR_ROWS + threadIdx.x;
@@ -86,14 +108,47 @@ ir_init_kernel(int n, int nrhs, double **dA_array, int ldda, float **dAs_array, 
     float *As = dAs_array[mat];
     double rs = 0.0;
     bool ovf = false;
-    if (i < n) {
+    if (i < n && rowscale != nullptr) {
+        // integer max of |a| (bit patterns order like magnitudes) and FP32 row sums
+        unsigned long long mbits = 0ull;
+        float rsf = 0.f;
         for (int j = 0; j < n; j++) {
             const double a = A[i + (size_t)j * ldda];
-            rs += fabs(a);
-            const float f = __double2float_rn(a);
-            ovf |= (isinf(f) && !isinf(a));
+            const unsigned long long ab = (unsigned long long)__double_as_longlong(a) &
+                                          0x7fffffffffffffffull;
+            mbits = ab > mbits ? ab : mbits;
+            rsf += fabsf(d2f_rn_int(a));
+        }
+        rowscale[(size_t)mat * n + i] = pow2_scale(__longlong_as_double((long long)mbits));
+        rs = (double)rsf;
+    }
+    if (i < n && rowscale == nullptr) {
+        // As = float(A) on the integer pipes; ||A||_inf as the FP32 row sums of
+        // |float(a_ij)| (j ascending), eight loads in flight per thread
+        float rsf = 0.f;
+        int j = 0;
+        for (; j + 8 <= n; j += 8) {
+            double a[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) a[u] = A[i + (size_t)(j + u) * ldda];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const float f = d2f_rn_int(a[u]);
+                rsf += fabsf(f);
+                ovf |= d2f_overflowed(a[u], f);
+                As[i + (size_t)(j + u) * ldas] = f;
+            }
+        }
+        for (; j < n; j++) {
+            const double a = A[i + (size_t)j * ldda];
+            const float f = d2f_rn_int(a);
+            rsf += fabsf(f);
+            ovf |= d2f_overflowed(a, f);
             As[i + (size_t)j * ldas] = f;
         }
+        rs = (double)rsf;
+    }
+    if (i < n) {
         const double *B = dB_array[mat];
         double *X = dX_array[mat];
         double *Rm = R + (size_t)mat * nrhs * n;
@@ -107,6 +162,27 @@ ir_init_kernel(int n, int nrhs, double **dA_array, int ldda, float **dAs_array, 
         st[1] = IR_FAILED;
         iter[mat] = -2;
     }
+}
+
+// FP16 factorisation: column scale 2^-f_j with max_i |a_ij| 2^-e_i 2^-f_j in
+// [0.5, 1), then As = float(a_ij 2^-e_i 2^-f_j).  One thread per column.
+__global__ void __launch_bounds__(128)
+ir_colscale_kernel(int n, double **dA_array, int ldda, float **dAs_array, int ldas,
+                   const double *rowscale, double *colscale)
+{
+    const int mat = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double *a = dA_array[mat] + (size_t)j * ldda;
+    const double *r = rowscale + (size_t)mat * n;
+    // scale factors are powers of two, so FP32 arithmetic on float(a) scales exactly
+    float cmax = 0.f;
+    for (int i = 0; i < n; i++) cmax = fmaxf(cmax, fabsf(d2f_rn_int(a[i])) * (float)r[i]);
+    const double c = pow2_scale((double)cmax);
+    colscale[(size_t)mat * n + j] = c;
+    const float cf = (float)c;
+    float *as = dAs_array[mat] + (size_t)j * ldas;
+    for (int i = 0; i < n; i++) as[i] = d2f_rn_int(a[i]) * ((float)r[i] * cf);
 }
 
 // Convergence test on the norms of parity `par`; called by one thread.
@@ -130,11 +206,13 @@ __device__ __forceinline__ bool ir_converged(const unsigned long long *st, int p
 }
 
 // check (when it >= 0) + correction solve X += float-solve(R) with the FP32
-// factors.  One CTA per (matrix, group of IR_SOLVE_NR right-hand sides).
+// factors.  One CTA per (matrix, group of NR right-hand sides).
+template <int NR>
 __global__ void __launch_bounds__(256)
 ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, int **ipiv_array,
                 double **dX_array, int lddx, const double *R, unsigned long long *stats,
-                int *iter, const int *info, int it, double tol)
+                int *iter, const int *info, int it, double tol, const double *rowscale,
+                const double *colscale)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *sB = reinterpret_cast<float *>(smem_raw);
@@ -160,19 +238,22 @@ ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, int **ipiv_array,
         unsigned long long *nx = norms_of(st, (it + 1) & 1);
         for (int e = tid; e < 2 * IR_NRHS_MAX + 2; e += blockDim.x) nx[e] = 0ull;
     }
-    const int c0 = blockIdx.x * IR_SOLVE_NR;
-    const int nr = min(IR_SOLVE_NR, nrhs - c0);
+    const int c0 = blockIdx.x * NR;
+    const int nr = min(NR, nrhs - c0);
     const double *Rm = R + ((size_t)mat * nrhs + c0) * n;
-    for (int e = tid; e < IR_SOLVE_NR * n; e += blockDim.x) {
+    for (int e = tid; e < NR * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
-        sB[c * n + i] = c < nr ? __double2float_rn(Rm[i + (size_t)c * n]) : 0.f;
+        const double rv = c < nr ? Rm[i + (size_t)c * n] : 0.0;
+        sB[c * n + i] = __double2float_rn(rowscale ? rv * rowscale[(size_t)mat * n + i] : rv);
     }
     __syncthreads();
-    solve_smem<float, false, IR_SOLVE_NR>(n, dAs_array[mat], ldas, ipiv_array[mat], sB, nr);
+    solve_smem<float, false, NR>(n, dAs_array[mat], ldas, ipiv_array[mat], sB, nr);
     double *X = dX_array[mat] + (size_t)c0 * lddx;
     for (int e = tid; e < nr * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
-        X[i + (size_t)c * lddx] = X[i + (size_t)c * lddx] + (double)sB[c * n + i];
+        const double d = (double)sB[c * n + i];
+        X[i + (size_t)c * lddx] = X[i + (size_t)c * lddx] +
+                                  (colscale ? d * colscale[(size_t)mat * n + i] : d);
     }
 }
 
@@ -290,11 +371,11 @@ __global__ void set_float_pointers(float **out, float *base, size_t stride, int 
 static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct IrLayout {
-    size_t stats, count, asp, as, r, ca, cp, cx, cidx, cinfo, total;
+    size_t stats, count, asp, as, r, ca, cp, cx, cidx, cinfo, rsc, csc, tc, tc_bytes, total;
     int ldas;
 };
 
-static IrLayout ir_layout(int n, int nrhs, int batch)
+static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900)
 {
     IrLayout L;
     L.ldas = (n + 31) & ~31;
@@ -309,6 +390,21 @@ static IrLayout ir_layout(int n, int nrhs, int batch)
     L.cx = o;    o = align256(o + (size_t)batch * sizeof(double *));
     L.cidx = o;  o = align256(o + (size_t)batch * sizeof(int));
     L.cinfo = o; o = align256(o + (size_t)batch * sizeof(int));
+    L.rsc = L.csc = L.tc = o;
+    L.tc_bytes = 0;
+    if (prec == 905) {
+        L.rsc = o; o = align256(o + (size_t)batch * n * sizeof(double));
+        L.csc = o; o = align256(o + (size_t)batch * n * sizeof(double));
+    }
+    if (prec != 900) {
+        size_t tcb = 0;
+        magma_sgetrf_batched_tc(prec, n, n, nullptr, mlu_max(1, (n + 31) & ~31), nullptr, nullptr,
+                                nullptr, &tcb, batch, nullptr);
+        o = (o + 1023) & ~(size_t)1023;
+        L.tc = o;
+        L.tc_bytes = tcb;
+        o = align256(o + tcb);
+    }
     L.total = o;
     return L;
 }
@@ -319,12 +415,8 @@ static void launch_residual(int n, int nrhs, double **dA, int ldda, double **dB,
                             int batch, cudaStream_t s)
 {
     const size_t smem = (size_t)n * NR * sizeof(double);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(ir_residual_kernel<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             200 * 1024);
-        attr = true;
-    }
+    static size_t dyn_max = 0;
+    if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(ir_residual_kernel<NR>);
     ir_residual_kernel<NR><<<dim3((n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS, smem, s>>>(
         n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par);
 }
@@ -344,13 +436,16 @@ static void residual(int n, int nrhs, double **dA, int ldda, double **dB, int ld
 
 using namespace mlu;
 
-extern "C" magma_int_t
-magma_dsgesv_batched_work(magma_int_t n, magma_int_t nrhs, double **dA_array, magma_int_t ldda,
-                          magma_int_t **dipiv_array, double **dB_array, magma_int_t lddb,
-                          double **dX_array, magma_int_t lddx, magma_int_t *dinfo_array,
-                          magma_int_t *diter_array, magma_int_t itermax, double tol,
-                          magma_int_t fallback, void *work, size_t *lwork,
-                          magma_int_t batchCount, magma_queue_t queue)
+// The refinement driver for factorisation precision `prec`: 900 FP32
+// (Magma_PREC_SS), 905 FP16 tensor-core updates (Magma_PREC_SHT, with
+// power-of-two row and column scaling), 930 BF16 tensor-core updates.
+// Argument positions in error codes are those of magma_dsgesv_batched_work.
+static magma_int_t
+ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrhs, double **dA_array,
+          magma_int_t ldda, magma_int_t **dipiv_array, double **dB_array, magma_int_t lddb,
+          double **dX_array, magma_int_t lddx, magma_int_t *dinfo_array, magma_int_t *diter_array,
+          magma_int_t itermax, double tol, magma_int_t fallback, void *work, size_t *lwork,
+          magma_int_t batchCount, magma_queue_t queue)
 {
     magma_int_t info = 0;
     if (n < 0) info = -1;
@@ -360,16 +455,24 @@ magma_dsgesv_batched_work(magma_int_t n, magma_int_t nrhs, double **dA_array, ma
     else if (lddx < mlu_max(1, n)) info = -9;
     else if (itermax < 0) info = -12;
     if (info != 0) {
-        magma_xerbla(__func__, -info);
-        return info;
+        magma_xerbla(name, -info + argoff);
+        return info - argoff;
     }
-    const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0));
+    const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0), prec);
     if (work == nullptr) {          // workspace query
         *lwork = L.total;
         return 0;
     }
     if (*lwork < L.total) return -15;
     if (n == 0 || nrhs == 0 || batchCount <= 0) return 0;
+    // shared-memory limits of the correction solve and the residual kernels
+    static size_t solve_dyn_max = 0;
+    if (!solve_dyn_max)
+        solve_dyn_max = min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR>),
+                            mlu_allow_dynamic_smem(ir_solve_kernel<4>));
+    if ((size_t)IR_SOLVE_NR * n * sizeof(float) > solve_dyn_max ||
+        (size_t)n * IR_NRHS_MAX * sizeof(double) > 200 * 1024)
+        return MAGMA_ERR_NOT_SUPPORTED;
 
     cudaStream_t s = queue->stream;
     char *w = (char *)work;
@@ -382,28 +485,44 @@ magma_dsgesv_batched_work(magma_int_t n, magma_int_t nrhs, double **dA_array, ma
     cudaMemsetAsync(w, 0, L.asp, s);   // stats, counters
     set_float_pointers<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(As_array, As,
                                                                      (size_t)n * L.ldas, batchCount);
+    double *rsc = prec == 905 ? (double *)(w + L.rsc) : nullptr;
+    double *csc = prec == 905 ? (double *)(w + L.csc) : nullptr;
     const dim3 rows_grid((n + IR_ROWS - 1) / IR_ROWS, batchCount);
     ir_init_kernel<<<rows_grid, IR_ROWS, 0, s>>>(n, nrhs, dA_array, ldda, As_array, L.ldas,
                                                  dB_array, lddb, dX_array, lddx, R, stats,
-                                                 diter_array);
-    magma_int_t rc = magma_sgetrf_batched(n, n, As_array, L.ldas, dipiv_array, dinfo_array,
-                                          batchCount, queue);
-    if (rc != 0) return rc;
-    const size_t ssmem = (size_t)IR_SOLVE_NR * n * sizeof(float);
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(ir_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr = true;
+                                                 diter_array, rsc);
+    if (rsc)
+        ir_colscale_kernel<<<dim3((n + 127) / 128, batchCount), 128, 0, s>>>(
+            n, dA_array, ldda, As_array, L.ldas, rsc, csc);
+    magma_int_t rc;
+    if (prec == 900) {
+        rc = magma_sgetrf_batched(n, n, As_array, L.ldas, dipiv_array, dinfo_array, batchCount,
+                                  queue);
+    } else {
+        size_t tcb = L.tc_bytes;
+        rc = magma_sgetrf_batched_tc(prec, n, n, As_array, L.ldas, dipiv_array, dinfo_array,
+                                     w + L.tc, &tcb, batchCount, queue);
     }
-    const dim3 solve_grid(mlu_ceildiv(nrhs, IR_SOLVE_NR), batchCount);
-    ir_solve_kernel<<<solve_grid, 256, ssmem, s>>>(n, nrhs, As_array, L.ldas, dipiv_array,
-                                                   dX_array, lddx, R, stats, diter_array,
-                                                   dinfo_array, -1, tol);
+    if (rc != 0) return rc;
+    // right-hand sides per solve CTA: 4 when they fit, else 8
+    const int snr = nrhs <= 4 ? 4 : IR_SOLVE_NR;
+    const size_t ssmem = (size_t)snr * n * sizeof(float);
+    auto solve = [&](int it) {
+        const dim3 grid(mlu_ceildiv(nrhs, snr), batchCount);
+        if (snr == 4)
+            ir_solve_kernel<4><<<grid, 256, ssmem, s>>>(n, nrhs, As_array, L.ldas, dipiv_array,
+                                                        dX_array, lddx, R, stats, diter_array,
+                                                        dinfo_array, it, tol, rsc, csc);
+        else
+            ir_solve_kernel<IR_SOLVE_NR><<<grid, 256, ssmem, s>>>(
+                n, nrhs, As_array, L.ldas, dipiv_array, dX_array, lddx, R, stats, diter_array,
+                dinfo_array, it, tol, rsc, csc);
+    };
+
+    solve(-1);
     residual(n, nrhs, dA_array, ldda, dB_array, lddb, dX_array, lddx, R, stats, 0, batchCount, s);
     for (int it = 0; it < itermax; it++) {
-        ir_solve_kernel<<<solve_grid, 256, ssmem, s>>>(n, nrhs, As_array, L.ldas, dipiv_array,
-                                                       dX_array, lddx, R, stats, diter_array,
-                                                       dinfo_array, it, tol);
+        solve(it);
         residual(n, nrhs, dA_array, ldda, dB_array, lddb, dX_array, lddx, R, stats, (it + 1) & 1,
                  batchCount, s);
     }
@@ -415,6 +534,8 @@ magma_dsgesv_batched_work(magma_int_t n, magma_int_t nrhs, double **dA_array, ma
     int failed = 0;
     cudaMemcpyAsync(&failed, count, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return MAGMA_ERR_UNKNOWN;
+    if (prec != 900 && magma_sgetrf_batched_tc_status(n, n, w + L.tc, batchCount, queue) != 0)
+        return MAGMA_ERR_UNKNOWN;   // a tensor-pipeline wait timed out
     if (failed == 0) return 0;
     double **cA = (double **)(w + L.ca);
     int **cP = (int **)(w + L.cp);
@@ -431,6 +552,37 @@ magma_dsgesv_batched_work(magma_int_t n, magma_int_t nrhs, double **dA_array, ma
                                                                     dinfo_array);
     MLU_CHECK_LAUNCH();
     return 0;
+}
+
+extern "C" magma_int_t
+magma_dsgesv_batched_work(magma_int_t n, magma_int_t nrhs, double **dA_array, magma_int_t ldda,
+                          magma_int_t **dipiv_array, double **dB_array, magma_int_t lddb,
+                          double **dX_array, magma_int_t lddx, magma_int_t *dinfo_array,
+                          magma_int_t *diter_array, magma_int_t itermax, double tol,
+                          magma_int_t fallback, void *work, size_t *lwork,
+                          magma_int_t batchCount, magma_queue_t queue)
+{
+    return ir_driver(__func__, 0, 900, n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb, dX_array,
+                     lddx, dinfo_array, diter_array, itermax, tol, fallback, work, lwork,
+                     batchCount, queue);
+}
+
+extern "C" magma_int_t
+magma_dxgesv_batched_work(magma_int_t precision, magma_int_t n, magma_int_t nrhs,
+                          double **dA_array, magma_int_t ldda, magma_int_t **dipiv_array,
+                          double **dB_array, magma_int_t lddb, double **dX_array,
+                          magma_int_t lddx, magma_int_t *dinfo_array, magma_int_t *diter_array,
+                          magma_int_t itermax, double tol, magma_int_t fallback, void *work,
+                          size_t *lwork, magma_int_t batchCount, magma_queue_t queue)
+{
+    if (precision != 900 && precision != 905 && precision != 930) {
+        magma_xerbla(__func__, 1);
+        return -1;
+    }
+    // argument i of magma_dsgesv_batched_work is argument i+1 here
+    return ir_driver(__func__, 1, precision, n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb,
+                     dX_array, lddx, dinfo_array, diter_array, itermax, tol, fallback, work, lwork,
+                     batchCount, queue);
 }
 
 extern "C" magma_int_t

@@ -1,0 +1,466 @@
+// lu_core.cuh -- the steps of one right-looking LU panel step as device
+// functions, shared by the per-step kernels of the fixed-size path
+// (lu_blocked.cu) and the persistent one-CTA-per-matrix kernel of the
+// variable-size path (lu_vbatched.cu).  Both therefore perform the same
+// floating-point operations in the same order as the CPU oracle.
+//
+// Restates, in one place: the fused panel (magmablas/zgetf2_kernels.cu:833-1058,
+// magmablas/zgetf2_devicefunc.cuh:218-294), the pivot bookkeeping
+// (magmablas/getrf_setup_pivinfo.cu:59-309), the row swaps
+// (magmablas/zlaswp_device.cuh:25-84), the TRSM of U12
+// (magmablas/ztrsm_batched_core.cpp) and the trailing update (cuBLAS dgemm in
+// the reference, magmablas/zgemm_batched.cpp:60-89).
+#pragma once
+#include "common.cuh"
+
+namespace mlu {
+
+constexpr int PANEL_NB = 32;          // largest panel width
+constexpr size_t PANEL_SMEM_MAX = 200 * 1024;   // shared memory for one panel
+constexpr int SWAP_W = 32;            // columns per gather/scatter chunk
+
+// ---------------------------------------------------------------------------
+// Panel factorisation of the pm x ib block at A (leading dimension lda) in
+// shared memory.  `smem` must hold pm*(ib+1) T plus 2*pm ints.  Every thread
+// of the block calls it.  On return the panel is written back in pivoted
+// order, s_ipiv[k] holds the pivot position (relative to the panel's first
+// row) chosen at column k, and the return value (valid in thread 0) is the
+// 1-based column of the first zero pivot plus `col0`, or 0.
+//
+// Rows stay where they were loaded; sPos[i] is row i's position in LAPACK's
+// current order and sRowAt the inverse.  Per column: per-thread then per-warp
+// arg-max of |a| (63-bit integer keys, ties to the smaller position, idamax's
+// NaN rule), one warp combines the warp winners and updates the maps, then
+// every thread scales and updates only its own rows -- two barriers per
+// column.
+template <typename T>
+__device__ __forceinline__ int panel_factor(int pm, int ib, T *A, int lda, unsigned char *smem, int *s_ipiv,
+                            int col0)
+{
+    __shared__ unsigned s_whi[32], s_wlo[32], s_wpos[32];
+    __shared__ int s_prow;
+    __shared__ T s_piv, s_rcp;
+    const int LDS = ib + 1;
+    T *sP = reinterpret_cast<T *>(smem);
+    int *sPos = reinterpret_cast<int *>(sP + (size_t)pm * LDS);
+    int *sRowAt = sPos + pm;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nthr = blockDim.x, nwarps = nthr >> 5;
+
+    for (int j = 0; j < ib; j++)
+        for (int i = tid; i < pm; i += nthr) sP[i * LDS + j] = A[i + (size_t)j * lda];
+    for (int i = tid; i < pm; i += nthr) { sPos[i] = i; sRowAt[i] = i; }
+    int info_local = 0;
+    __syncthreads();
+
+    for (int k = 0; k < ib; k++) {
+        unsigned long long best = 0ull;
+        unsigned bpos = 0xffffffffu;
+        for (int i = tid; i < pm; i += nthr) {
+            const int p = sPos[i];
+            if (p >= k) {
+                const T v = sP[i * LDS + k];
+                unsigned long long mag = Prec<T>::absbits(v);
+                if (Prec<T>::isnan_(v)) mag = (p == k) ? 0x7fffffffffffffffull : 0ull;
+                const unsigned long long key = mag | 0x8000000000000000ull;
+                if (key > best || (key == best && (unsigned)p < bpos)) { best = key; bpos = p; }
+            }
+        }
+        {
+            const unsigned hi = (unsigned)(best >> 32), lo = (unsigned)best;
+            const unsigned mhi = __reduce_max_sync(FULL, hi);
+            const unsigned mlo = __reduce_max_sync(FULL, hi == mhi ? lo : 0u);
+            const bool cand = hi == mhi && lo == mlo;
+            const unsigned wpos = __reduce_min_sync(FULL, cand ? bpos : 0xffffffffu);
+            if (lane == 0) { s_whi[warp] = mhi; s_wlo[warp] = mlo; s_wpos[warp] = wpos; }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const unsigned hi = lane < nwarps ? s_whi[lane] : 0u;
+            const unsigned lo = lane < nwarps ? s_wlo[lane] : 0u;
+            const unsigned ps = lane < nwarps ? s_wpos[lane] : 0xffffffffu;
+            const unsigned mhi = __reduce_max_sync(FULL, hi);
+            const unsigned mlo = __reduce_max_sync(FULL, hi == mhi ? lo : 0u);
+            const unsigned P = __reduce_min_sync(FULL, (hi == mhi && lo == mlo) ? ps : 0xffffffffu);
+            if (lane == 0) {
+                const int prow = sRowAt[P];
+                const int qrow = sRowAt[k];
+                const T piv = sP[prow * LDS + k];
+                sPos[prow] = k;
+                sRowAt[k] = prow;
+                if (qrow != prow) { sPos[qrow] = P; sRowAt[P] = qrow; }
+                s_prow = prow;
+                s_piv = piv;
+                s_rcp = T(1) / piv;
+                s_ipiv[k] = (int)P;
+                if (!Prec<T>::nonzero(piv) && info_local == 0) info_local = col0 + k + 1;
+            }
+        }
+        __syncthreads();
+        const int prow = s_prow;
+        const T piv = s_piv, r = s_rcp;
+        const bool nz = Prec<T>::nonzero(piv);
+        for (int i = tid; i < pm; i += nthr) {
+            if (sPos[i] > k) {
+                T *row = sP + i * LDS;
+                const T v = row[k];
+                const T l = nz ? rscale(v, piv, r) : v;
+                row[k] = l;
+                const T *prw = sP + prow * LDS;
+                for (int j = k + 1; j < ib; j++) row[j] = Prec<T>::fma_(-l, prw[j], row[j]);
+            }
+        }
+    }
+    __syncthreads();
+    for (int j = 0; j < ib; j++)
+        for (int i = tid; i < pm; i += nthr) A[sPos[i] + (size_t)j * lda] = sP[i * LDS + j];
+    __syncthreads();
+    return info_local;
+}
+
+// ---------------------------------------------------------------------------
+// Register-resident panel factorisation, same arithmetic as panel_factor.
+// Thread t owns rows t, t + nthr, ... (RPT of them, pm <= RPT * nthr) with
+// all ib <= 32 panel columns in registers.  One barrier per column: each warp
+// publishes its best candidate row (key, position, the row itself) into a
+// slot of a double-buffered table, then every thread reduces the table on its
+// own, so all threads agree on the pivot without a second barrier.  Row
+// positions live in registers of the owning thread.  Returns the first zero
+// pivot column + col0 (1-based) or 0, valid in thread 0; s_ipiv as in
+// panel_factor.  nthr must be a multiple of 32 and at most 1024.
+template <typename T, int RPT>
+__device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, int *s_ipiv,
+                                                 int col0)
+{
+    __shared__ unsigned s_hi[2][32], s_lo[2][32], s_pos[2][32];
+    __shared__ T s_row[2][32][PANEL_NB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nthr = blockDim.x, nwarps = nthr >> 5;
+
+    T a[RPT][PANEL_NB];
+    int pos[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; r++) {
+        const int i = tid + r * nthr;
+        pos[r] = i < pm ? i : 0x7fffffff;          // rows past pm never become active
+#pragma unroll
+        for (int j = 0; j < PANEL_NB; j++)
+            a[r][j] = (i < pm && j < ib) ? A[i + (size_t)j * lda] : T(0);
+    }
+    int info_local = 0;
+
+#pragma unroll
+    for (int k = 0; k < PANEL_NB; k++) {
+        if (k >= ib) break;
+        const int buf = k & 1;
+        // best active row of this thread: largest key, ties to the smaller position
+        unsigned long long best = 0ull;
+        unsigned bpos = 0xffffffffu;
+        int bslot = 0;
+#pragma unroll
+        for (int r = 0; r < RPT; r++) {
+            if (pos[r] >= k && pos[r] != 0x7fffffff) {
+                const T v = a[r][k];
+                unsigned long long mag = Prec<T>::absbits(v);
+                if (Prec<T>::isnan_(v)) mag = (pos[r] == k) ? 0x7fffffffffffffffull : 0ull;
+                const unsigned long long key = mag | 0x8000000000000000ull;
+                if (key > best || (key == best && (unsigned)pos[r] < bpos)) {
+                    best = key; bpos = pos[r]; bslot = r;
+                }
+            }
+        }
+        const unsigned hi = (unsigned)(best >> 32), lo = (unsigned)best;
+        const unsigned mhi = __reduce_max_sync(FULL, hi);
+        const unsigned mlo = __reduce_max_sync(FULL, hi == mhi ? lo : 0u);
+        const bool cand = hi == mhi && lo == mlo;
+        const unsigned wpos = __reduce_min_sync(FULL, cand ? bpos : 0xffffffffu);
+        const bool winner = cand && bpos == wpos && mhi != 0u;
+        if (lane == 0) { s_hi[buf][warp] = mhi; s_lo[buf][warp] = mlo; s_pos[buf][warp] = wpos; }
+        if (winner) {
+#pragma unroll
+            for (int j = 0; j < PANEL_NB; j++) {
+                T v = a[0][j];
+#pragma unroll
+                for (int r = 1; r < RPT; r++) v = (bslot == r) ? a[r][j] : v;
+                s_row[buf][warp][j] = v;
+            }
+        }
+        __syncthreads();
+        // every thread reduces the warp winners
+        unsigned ghi = 0, glo = 0, gpos = 0xffffffffu;
+        int gw = 0;
+#pragma unroll
+        for (int w = 0; w < 32; w++) {
+            if (w < nwarps) {
+                const unsigned h = s_hi[buf][w], l = s_lo[buf][w], p = s_pos[buf][w];
+                if (h > ghi || (h == ghi && (l > glo || (l == glo && p < gpos)))) {
+                    ghi = h; glo = l; gpos = p; gw = w;
+                }
+            }
+        }
+        const T *prow = s_row[buf][gw];
+        const T piv = prow[k];
+        const bool nz = Prec<T>::nonzero(piv);
+        const T rcp = T(1) / piv;
+        if (tid == 0) {
+            s_ipiv[k] = (int)gpos;
+            if (!nz && info_local == 0) info_local = col0 + k + 1;
+        }
+        // interchange of positions k and gpos, then scale and update own rows
+#pragma unroll
+        for (int r = 0; r < RPT; r++) {
+            if (pos[r] == (int)gpos) pos[r] = k;
+            else if (pos[r] == k) pos[r] = (int)gpos;
+        }
+#pragma unroll
+        for (int r = 0; r < RPT; r++) {
+            if (pos[r] > k && pos[r] != 0x7fffffff) {
+                const T v = a[r][k];
+                const T l = nz ? rscale(v, piv, rcp) : v;
+                a[r][k] = l;
+#pragma unroll
+                for (int j = k + 1; j < PANEL_NB; j++)
+                    if (j < ib) a[r][j] = Prec<T>::fma_(-l, prow[j], a[r][j]);
+            }
+        }
+    }
+    // write back in pivoted order
+#pragma unroll
+    for (int r = 0; r < RPT; r++) {
+        if (pos[r] != 0x7fffffff) {
+#pragma unroll
+            for (int j = 0; j < PANEL_NB; j++)
+                if (j < ib) A[pos[r] + (size_t)j * lda] = a[r][j];
+        }
+    }
+    __syncthreads();
+    return info_local;
+}
+
+// ---------------------------------------------------------------------------
+// Compound permutation of the sequential interchanges k = j0..j0+ib-1 with
+// targets ipiv[k]-1 (1-based ipiv).  Built by warp 0 (threads 0..31 must call
+// it) with ballots over a 64-entry table: s_row[e] is a touched row, s_src[e]
+// the row whose original content ends up there.  The caller synchronises
+// before using the table.
+__device__ __forceinline__ void build_permutation(const int *ipiv, int j0, int ib, int *s_row, int *s_src,
+                                         int *s_cnt)
+{
+    const int lane = threadIdx.x & 31;
+    // all ib targets in one coalesced load, then broadcast by shuffles
+    const int my_target = lane < ib ? ipiv[j0 + lane] - 1 : 0;
+    int cnt = 0;
+    int r0 = -1, r1 = -1, s0 = -1, s1 = -1;   // this lane's entries lane and lane+32
+    for (int k = 0; k < ib; k++) {
+        const int a = j0 + k, b = __shfl_sync(FULL, my_target, k);
+        if (a == b) continue;
+        unsigned fa0 = __ballot_sync(FULL, r0 == a), fa1 = __ballot_sync(FULL, r1 == a);
+        int ia = fa0 ? __ffs(fa0) - 1 : (fa1 ? 32 + __ffs(fa1) - 1 : -1);
+        if (ia < 0) {
+            ia = cnt++;
+            if (lane == (ia & 31)) { if (ia < 32) { r0 = a; s0 = a; } else { r1 = a; s1 = a; } }
+        }
+        unsigned fb0 = __ballot_sync(FULL, r0 == b), fb1 = __ballot_sync(FULL, r1 == b);
+        int ibb = fb0 ? __ffs(fb0) - 1 : (fb1 ? 32 + __ffs(fb1) - 1 : -1);
+        if (ibb < 0) {
+            ibb = cnt++;
+            if (lane == (ibb & 31)) { if (ibb < 32) { r0 = b; s0 = b; } else { r1 = b; s1 = b; } }
+        }
+        const int va = __shfl_sync(FULL, ia < 32 ? s0 : s1, ia & 31);
+        const int vb = __shfl_sync(FULL, ibb < 32 ? s0 : s1, ibb & 31);
+        if (lane == (ia & 31)) { if (ia < 32) s0 = vb; else s1 = vb; }
+        if (lane == (ibb & 31)) { if (ibb < 32) s0 = va; else s1 = va; }
+    }
+    s_row[lane] = r0; s_src[lane] = s0;
+    s_row[lane + 32] = r1; s_src[lane + 32] = s1;
+    if (lane == 0) *s_cnt = cnt;
+}
+
+// Moves the touched rows of columns [c0, c1) of A (ld lda): gather all sources
+// into s_tmp (2*PANEL_NB x (SWAP_W+1)), then scatter, SWAP_W columns at a time.
+// All threads call it; it synchronises internally.
+template <typename T>
+__device__ __forceinline__ void apply_permutation(T *A, int lda, int c0, int c1, const int *s_row, const int *s_src,
+                                  int cnt, T *s_tmp)
+{
+    // rows run fastest across threads, so runs of adjacent rows coalesce
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    if (cnt == 0) return;
+    for (int cb = c0; cb < c1; cb += SWAP_W) {
+        const int w = min(SWAP_W, c1 - cb);
+        for (int e = tid; e < cnt * w; e += nthr) {
+            const int pr = e % cnt, c = e / cnt;
+            s_tmp[pr * (SWAP_W + 1) + c] = A[s_src[pr] + (size_t)(cb + c) * lda];
+        }
+        __syncthreads();
+        for (int e = tid; e < cnt * w; e += nthr) {
+            const int pr = e % cnt, c = e / cnt;
+            A[s_row[pr] + (size_t)(cb + c) * lda] = s_tmp[pr * (SWAP_W + 1) + c];
+        }
+        __syncthreads();
+    }
+}
+
+// U12 = L11^{-1} A12 for the columns [c0, c1) of the ib rows starting at row
+// j0 (L11 unit lower, at (j0, j0)).  One thread per column, rows in registers,
+// t ascending.  All threads call it; it synchronises on entry and exit.
+template <typename T>
+__device__ __forceinline__ void trsm_l11(T *A, int lda, int j0, int ib, int c0, int c1)
+{
+    __shared__ T s_L[PANEL_NB][PANEL_NB + 1];
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    for (int e = tid; e < ib * ib; e += nthr) {
+        const int i = e % ib, t = e / ib;
+        s_L[i][t] = A[j0 + i + (size_t)(j0 + t) * lda];
+    }
+    __syncthreads();
+    for (int cb = c0; cb < c1; cb += nthr) {
+        if (cb + tid < c1) {
+            T *col = A + j0 + (size_t)(cb + tid) * lda;
+            T u[PANEL_NB];
+#pragma unroll
+            for (int i = 0; i < PANEL_NB; i++) u[i] = i < ib ? col[i] : T(0);
+#pragma unroll
+            for (int t = 0; t < PANEL_NB; t++) {
+                if (t >= ib) break;
+#pragma unroll
+                for (int i = t + 1; i < PANEL_NB; i++)
+                    if (i < ib) u[i] = Prec<T>::fma_(-s_L[i][t], u[t], u[i]);
+            }
+#pragma unroll
+            for (int i = 0; i < PANEL_NB; i++) if (i < ib) col[i] = u[i];
+        }
+    }
+    __syncthreads();
+}
+
+// U12 = L11^{-1} A12 as trsm_l11, with the right-hand sides staged in shared
+// memory (sbuf: PANEL_NB x chunk T) instead of registers: one thread per
+// column, t ascending, so the arithmetic is that of trsm_l11 while the
+// kernel stays light on registers.  All threads call it.
+template <typename T>
+__device__ __forceinline__ void trsm_l11_smem(T *A, int lda, int j0, int ib, int c0, int c1,
+                                              T *sbuf, int chunk)
+{
+    __shared__ T s_L[PANEL_NB][PANEL_NB + 1];
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    for (int e = tid; e < ib * ib; e += nthr) {
+        const int i = e % ib, t = e / ib;
+        s_L[i][t] = A[j0 + i + (size_t)(j0 + t) * lda];
+    }
+    for (int cb = c0; cb < c1; cb += chunk) {
+        const int w = min(chunk, c1 - cb);
+        __syncthreads();
+        for (int e = tid; e < ib * w; e += nthr) {
+            const int i = e % ib, c = e / ib;           // coalesced down each column
+            sbuf[i * chunk + c] = A[j0 + i + (size_t)(cb + c) * lda];
+        }
+        __syncthreads();
+        for (int c = tid; c < w; c += nthr) {
+            for (int t = 0; t < ib; t++) {
+                const T ut = sbuf[t * chunk + c];
+                for (int i = t + 1; i < ib; i++)
+                    sbuf[i * chunk + c] = Prec<T>::fma_(-s_L[i][t], ut, sbuf[i * chunk + c]);
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < ib * w; e += nthr) {
+            const int i = e % ib, c = e / ib;
+            A[j0 + i + (size_t)(cb + c) * lda] = sbuf[i * chunk + c];
+        }
+    }
+    __syncthreads();
+}
+
+// The rest of one panel step done by the CTA that factored the panel: write
+// the pivots, apply the panel's interchanges to every column outside the
+// panel, and solve U12 = L11^{-1} A12 for the columns right of it.  A is the
+// matrix base, ipiv its pivot vector; s_ipiv holds the panel's local pivot
+// positions.  All threads call it (it synchronises internally).
+template <typename T>
+__device__ __forceinline__ void finish_panel_step(T *A, int lda, int n, int j0, int ib, int *ipiv,
+                                                  const int *s_ipiv, T *sbuf, int chunk)
+{
+    __shared__ int s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt;
+    __shared__ T s_tmp[2 * PANEL_NB * (SWAP_W + 1)];
+    if (threadIdx.x < ib) ipiv[j0 + threadIdx.x] = j0 + s_ipiv[threadIdx.x] + 1;
+    __syncthreads();
+    if (threadIdx.x < 32) build_permutation(ipiv, j0, ib, s_row, s_src, &s_cnt);
+    __syncthreads();
+    const int cnt = s_cnt;
+    apply_permutation<T>(A, lda, 0, j0, s_row, s_src, cnt, s_tmp);
+    apply_permutation<T>(A, lda, j0 + ib, n, s_row, s_src, cnt, s_tmp);
+    if (j0 + ib < n) trsm_l11_smem<T>(A, lda, j0, ib, j0 + ib, n, sbuf, chunk);
+}
+
+// One BM x BN tile of A22 -= L21 * U12 with rows from r0 and columns from c0
+// (rows >= m or columns >= n skipped).  L21 columns j0..j0+ib, U12 rows
+// j0..j0+ib.  sL, sU: PANEL_NB x BM and PANEL_NB x BN T.  Called by exactly
+// (BM/TM)*(BN/TN) threads; synchronises on entry and exit.
+template <typename T, int BM, int BN, int TM, int TN>
+__device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, int ib, int r0, int c0, T *sL,
+                          T *sU)
+{
+    constexpr int NT = (BM / TM) * (BN / TN);
+    const int tid = threadIdx.x;
+    __syncthreads();
+    for (int e = tid; e < ib * BM; e += NT) {
+        const int i = e % BM, k = e / BM;
+        sL[k * BM + i] = (r0 + i < m) ? A[r0 + i + (size_t)(j0 + k) * lda] : T(0);
+    }
+    for (int e = tid; e < ib * BN; e += NT) {
+        const int k = e % ib, j = e / ib;
+        sU[k * BN + j] = (c0 + j < n) ? A[j0 + k + (size_t)(c0 + j) * lda] : T(0);
+    }
+    const int tr = tid % (BM / TM), tc = tid / (BM / TM);
+    T acc[TM][TN];
+#pragma unroll
+    for (int b = 0; b < TN; b++) {
+        const int c = c0 + tc * TN + b;
+#pragma unroll
+        for (int a = 0; a < TM; a++) {
+            const int r = r0 + tr * TM + a;
+            acc[a][b] = (r < m && c < n) ? A[r + (size_t)c * lda] : T(0);
+        }
+    }
+    __syncthreads();
+    for (int k = 0; k < ib; k++) {
+        T l[TM], u[TN];
+#pragma unroll
+        for (int a = 0; a < TM; a++) l[a] = sL[k * BM + tr * TM + a];
+#pragma unroll
+        for (int b = 0; b < TN; b++) u[b] = sU[k * BN + tc * TN + b];
+#pragma unroll
+        for (int a = 0; a < TM; a++)
+#pragma unroll
+            for (int b = 0; b < TN; b++) acc[a][b] = Prec<T>::fma_(-l[a], u[b], acc[a][b]);
+    }
+#pragma unroll
+    for (int b = 0; b < TN; b++) {
+        const int c = c0 + tc * TN + b;
+#pragma unroll
+        for (int a = 0; a < TM; a++) {
+            const int r = r0 + tr * TM + a;
+            if (r < m && c < n) A[r + (size_t)c * lda] = acc[a][b];
+        }
+    }
+}
+
+// Panel width for a panel of pm rows whose shared-memory copy must fit in
+// `budget` bytes: 32, halved until it fits (at least 1).
+template <typename T>
+__host__ __device__ inline int panel_width(int pm, int want, size_t budget)
+{
+    int ib = want;
+    while (ib > 1 && (size_t)pm * (ib + 1) * sizeof(T) + 2 * (size_t)pm * sizeof(int) > budget)
+        ib >>= 1;
+    return ib;
+}
+
+template <typename T>
+__host__ __device__ inline size_t panel_smem_bytes(int pm, int ib)
+{
+    return (size_t)pm * (ib + 1) * sizeof(T) + 2 * (size_t)pm * sizeof(int);
+}
+
+}  // namespace mlu

@@ -1,0 +1,475 @@
+// lu_vbatched.cu -- variable-size batched LU factorisation and solve.
+//
+// Replaces magma_dgetrf_vbatched and its _max_nocheck_work variant
+// (src/zgetrf_vbatched.cpp:20-398: host-side checker and max reductions with
+// two device-to-host copies, cudaMalloc'ed workspace, and a host loop of
+// panel / swap / trsm / gemm launches whose grids are sized for the largest
+// matrix) and adds the solve, which MAGMA does not have for variable sizes:
+// magma_dgetrs_vbatched and magma_dgesv_vbatched.
+//
+// Design: one persistent launch does the whole factorisation (and solve).
+//   1. vb_sort_kernel (one CTA): counting sort of the matrices by size,
+//      largest first, into a work list -- no host round trip;
+//   2. vb_lu_kernel: every CTA repeatedly takes the next matrix of the list
+//      (atomic counter) and runs its complete blocked LU -- panel in shared
+//      memory, interchanges applied to the other columns and to the
+//      right-hand sides, TRSM, 64x64 trailing-update tiles -- then the
+//      triangular solves.  Largest-first order keeps the SMs evenly loaded to
+//      the end (longest-processing-time scheduling).
+// The steps are the device functions of lu_core.cuh, so factors, pivots and
+// solutions are bit-identical to the fixed-size path and to the CPU oracle.
+// The _max_nocheck_work entry points never allocate or synchronise and can
+// be captured in a CUDA graph.
+#include "common.cuh"
+#include "lu_core.cuh"
+#include "solve_core.cuh"
+
+namespace mlu {
+
+constexpr int VB_THREADS = 256;
+constexpr int VB_BINS = 1024;
+constexpr int VB_NR = 16;                  // right-hand sides per solve pass
+constexpr size_t VB_SMEM_CAP = 220 * 1024;
+
+__device__ __forceinline__ int vb_key(int m, int n) { return min(max(max(m, n), 0), VB_BINS - 1); }
+
+// order[] = matrix indices sorted by decreasing max(m,n); counter = 0.
+__global__ void __launch_bounds__(1024)
+vb_sort_kernel(const int *m_arr, const int *n_arr, int batch, int *order, int *counter)
+{
+    __shared__ int hist[VB_BINS];
+    __shared__ int warp_tot[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < VB_BINS; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    for (int k = tid; k < batch; k += blockDim.x) atomicAdd(&hist[vb_key(m_arr[k], n_arr[k])], 1);
+    __syncthreads();
+    // exclusive scan over bins in descending key order (thread t <-> bin VB_BINS-1-t)
+    const int bin = VB_BINS - 1 - tid;
+    const int v = hist[bin];
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(FULL, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = warp_tot[lane];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(FULL, w, d);
+            if (lane >= d) w += y;
+        }
+        warp_tot[lane] = w - warp_tot[lane];   // exclusive warp offsets
+    }
+    __syncthreads();
+    hist[bin] = warp_tot[warp] + x - v;        // exclusive offset of this bin
+    __syncthreads();
+    for (int k = tid; k < batch; k += blockDim.x) {
+        const int pos = atomicAdd(&hist[vb_key(m_arr[k], n_arr[k])], 1);
+        order[pos] = k;
+    }
+    if (tid == 0) *counter = 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(VB_THREADS)
+vb_lu_kernel(const int *m_arr, const int *n_arr, const int *nrhs_arr, T **dA_array,
+             const int *ldda_arr, int **ipiv_array, T **dB_array, const int *lddb_arr,
+             int *info_array, const int *order, int *counter, int batch, int smem_bytes)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int s_item, s_ipiv[PANEL_NB], s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    T *sT = reinterpret_cast<T *>(smem);
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(counter, 1);
+        __syncthreads();
+        const int idx = s_item;
+        if (idx >= batch) break;
+        const int k = order[idx];
+        const int m = m_arr[k], n = n_arr[k], lda = ldda_arr[k];
+        const int nrhs = nrhs_arr ? nrhs_arr[k] : 0;
+        T *A = dA_array[k];
+        int *ipiv = ipiv_array[k];
+        T *B = nrhs > 0 ? dB_array[k] : nullptr;
+        const int ldb = nrhs > 0 ? lddb_arr[k] : 1;
+        const int mn = min(m, n);
+        int info = 0;
+        for (int j0 = 0; j0 < mn;) {
+            const int pm = m - j0;
+            // register-resident panel when it fits (pm <= 512), else shared memory
+            const int ib = pm <= 2 * VB_THREADS ? min(PANEL_NB, mn - j0)
+                                                : panel_width<T>(pm, min(PANEL_NB, mn - j0),
+                                                                 (size_t)smem_bytes);
+            T *Ap = A + j0 + (size_t)j0 * lda;
+            const int il = pm <= VB_THREADS       ? panel_factor_regs<T, 1>(pm, ib, Ap, lda, s_ipiv, j0)
+                           : pm <= 2 * VB_THREADS ? panel_factor_regs<T, 2>(pm, ib, Ap, lda, s_ipiv, j0)
+                                                  : panel_factor<T>(pm, ib, Ap, lda, smem, s_ipiv, j0);
+            if (info == 0) info = il;
+            if (tid < ib) ipiv[j0 + tid] = j0 + s_ipiv[tid] + 1;
+            __syncthreads();
+            if (warp == 0) build_permutation(ipiv, j0, ib, s_row, s_src, &s_cnt);
+            __syncthreads();
+            const int cnt = s_cnt;
+            if (cnt > 0) {
+                apply_permutation<T>(A, lda, 0, j0, s_row, s_src, cnt, sT);
+                apply_permutation<T>(A, lda, j0 + ib, n, s_row, s_src, cnt, sT);
+                if (nrhs > 0) apply_permutation<T>(B, ldb, 0, nrhs, s_row, s_src, cnt, sT);
+            }
+            if (j0 + ib < n) {
+                trsm_l11_smem<T>(A, lda, j0, ib, j0 + ib, n, sT, 64);
+                const int rm = m - j0 - ib, rn = n - j0 - ib;
+                T *sL = sT, *sU = sT + PANEL_NB * 64;
+                for (int tn = 0; tn < rn; tn += 64)
+                    for (int tm = 0; tm < rm; tm += 64)
+                        gemm_tile<T, 64, 64, 4, 4>(A, lda, m, n, j0, ib, j0 + ib + tm, j0 + ib + tn,
+                                                   sL, sU);
+                __syncthreads();
+            }
+            j0 += ib;
+        }
+        if (tid == 0) info_array[k] = info;
+        if (nrhs > 0 && m == n && n > 0) {
+            for (int c0 = 0; c0 < nrhs; c0 += VB_NR) {
+                const int nr = min(VB_NR, nrhs - c0);
+                T *Bc = B + (size_t)c0 * ldb;
+                __syncthreads();
+                for (int e = tid; e < VB_NR * n; e += VB_THREADS) {
+                    const int c = e / n, i = e % n;
+                    sT[c * n + i] = c < nr ? Bc[i + (size_t)c * ldb] : T(0);
+                }
+                __syncthreads();
+                solve_smem<T, false, VB_NR>(n, A, lda, nullptr, sT, nr);
+                for (int e = tid; e < nr * n; e += VB_THREADS) {
+                    const int c = e / n, i = e % n;
+                    Bc[i + (size_t)c * ldb] = sT[c * n + i];
+                }
+            }
+        }
+    }
+}
+
+// Solve with existing factors, one CTA per (matrix, group of VB_NR columns).
+template <typename T, bool TRANS>
+__global__ void __launch_bounds__(VB_THREADS)
+vb_getrs_kernel(const int *n_arr, const int *nrhs_arr, T **dA_array, const int *ldda_arr,
+                int **ipiv_array, T **dB_array, const int *lddb_arr)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    T *sB = reinterpret_cast<T *>(smem);
+    const int k = blockIdx.y, tid = threadIdx.x;
+    const int n = n_arr[k], nrhs = nrhs_arr[k];
+    const int c0 = blockIdx.x * VB_NR;
+    if (n <= 0 || c0 >= nrhs) return;
+    const int nr = min(VB_NR, nrhs - c0);
+    const int ldb = lddb_arr[k];
+    T *B = dB_array[k] + (size_t)c0 * ldb;
+    for (int e = tid; e < VB_NR * n; e += VB_THREADS) {
+        const int c = e / n, i = e % n;
+        sB[c * n + i] = c < nr ? B[i + (size_t)c * ldb] : T(0);
+    }
+    __syncthreads();
+    solve_smem<T, TRANS, VB_NR>(n, dA_array[k], ldda_arr[k], ipiv_array[k], sB, nr);
+    for (int e = tid; e < nr * n; e += VB_THREADS) {
+        const int c = e / n, i = e % n;
+        B[i + (size_t)c * ldb] = sB[c * n + i];
+    }
+}
+
+// argument check + maxima, one small kernel: stats = {err_m, err_n, err_ldda, err_lddb,
+// max_m, max_n, max_nrhs, err_nrhs}
+__global__ void vb_check_kernel(const int *m, const int *n, const int *nrhs, const int *ldda,
+                                const int *lddb, int batch, int *stats)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= batch) return;
+    const int mk = m[k], nk = n[k], rk = nrhs ? nrhs[k] : 0;
+    if (mk < 0) stats[0] = 1;
+    if (nk < 0) stats[1] = 1;
+    if (rk < 0) stats[7] = 1;
+    if (ldda[k] < max(1, mk)) stats[2] = 1;
+    if (lddb && lddb[k] < max(1, nk)) stats[3] = 1;
+    atomicMax(&stats[4], mk);
+    atomicMax(&stats[5], nk);
+    atomicMax(&stats[6], rk);
+}
+
+template <typename T>
+size_t vb_smem_bytes(int max_m, int max_n, int max_nrhs)
+{
+    size_t need = 0;
+    const int pm = max(max_m, 1);
+    if (pm > 2 * VB_THREADS)   // shorter panels live in registers
+        need = max(need, panel_smem_bytes<T>(pm, min(PANEL_NB, max(min(max_m, max_n), 1))));
+    need = max(need, (size_t)2 * PANEL_NB * (SWAP_W + 1) * sizeof(T));
+    need = max(need, (size_t)2 * PANEL_NB * 64 * sizeof(T));
+    if (max_nrhs > 0) need = max(need, (size_t)VB_NR * max_n * sizeof(T));
+    return min(need, VB_SMEM_CAP);
+}
+
+inline size_t vb_work_bytes(int batch) { return ((size_t)batch * sizeof(int) + 16 + 255) & ~(size_t)255; }
+
+template <typename T>
+magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int max_n, int max_nrhs,
+                   T **dA, const int *ldda, int **ipiv, T **dB, const int *lddb, int *info,
+                   void *work, int batch, magma_queue_t q)
+{
+    if (batch <= 0) return 0;
+    static size_t dyn_max = 0;
+    if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(vb_lu_kernel<T>);
+    const size_t smem = min(vb_smem_bytes<T>(max_m, max_n, max_nrhs), dyn_max);
+    // the panel of the largest matrix must fit with at least width 1
+    if (max_m > 2 * VB_THREADS && panel_smem_bytes<T>(max_m, 1) > smem)
+        return MAGMA_ERR_NOT_SUPPORTED;
+    if ((size_t)2 * PANEL_NB * 64 * sizeof(T) > smem) return MAGMA_ERR_NOT_SUPPORTED;
+    if (max_nrhs > 0 && (size_t)VB_NR * max_n * sizeof(T) > smem) return MAGMA_ERR_NOT_SUPPORTED;
+    int *order = (int *)work;
+    int *counter = (int *)((char *)work + vb_work_bytes(batch) - 16);
+    vb_sort_kernel<<<1, 1024, 0, q->stream>>>(m, n, batch, order, counter);
+    int dev = q->device, sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vb_lu_kernel<T>, VB_THREADS, smem);
+    const int grid = max(1, min(batch, sms * max(per_sm, 1)));
+    vb_lu_kernel<T><<<grid, VB_THREADS, smem, q->stream>>>(m, n, nrhs, dA, ldda, ipiv, dB, lddb, info,
+                                                          order, counter, batch, (int)smem);
+    MLU_CHECK_LAUNCH();
+    return 0;
+}
+
+template <typename T>
+magma_int_t vb_getrs_run(bool trans, const int *n, const int *nrhs, int max_n, int max_nrhs, T **dA,
+                         const int *ldda, int **ipiv, T **dB, const int *lddb, int batch,
+                         magma_queue_t q)
+{
+    if (batch <= 0 || max_n <= 0 || max_nrhs <= 0) return 0;
+    const size_t smem = (size_t)VB_NR * max_n * sizeof(T);
+    if (smem > VB_SMEM_CAP) return MAGMA_ERR_NOT_SUPPORTED;
+    static size_t dyn_max[2] = {0, 0};
+    if (!dyn_max[trans])
+        dyn_max[trans] = trans ? mlu_allow_dynamic_smem(vb_getrs_kernel<T, true>)
+                               : mlu_allow_dynamic_smem(vb_getrs_kernel<T, false>);
+    if (smem > dyn_max[trans]) return MAGMA_ERR_NOT_SUPPORTED;
+    for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
+        const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
+        dim3 grid((max_nrhs + VB_NR - 1) / VB_NR, nb);
+        if (trans)
+            vb_getrs_kernel<T, true><<<grid, VB_THREADS, smem, q->stream>>>(
+                n + b0, nrhs + b0, dA + b0, ldda + b0, ipiv + b0, dB + b0, lddb + b0);
+        else
+            vb_getrs_kernel<T, false><<<grid, VB_THREADS, smem, q->stream>>>(
+                n + b0, nrhs + b0, dA + b0, ldda + b0, ipiv + b0, dB + b0, lddb + b0);
+    }
+    MLU_CHECK_LAUNCH();
+    return 0;
+}
+
+// Synchronous argument check and maxima (the reference's checker + setup,
+// magmablas/vbatched_check.cu:39-58, magmablas/vbatched_aux.cu:27-87).
+static magma_int_t vb_check(const int *m, const int *n, const int *nrhs, const int *ldda,
+                            const int *lddb, int batch, magma_queue_t q, int out[8])
+{
+    for (int i = 0; i < 8; i++) out[i] = 0;
+    if (batch <= 0) return 0;
+    int *stats = nullptr;
+    if (q->work_bytes < 64) {
+        if (q->work) { cudaStreamSynchronize(q->stream); cudaFree(q->work); }
+        q->work = nullptr;
+        q->work_bytes = 0;
+        if (cudaMalloc(&q->work, 64) != cudaSuccess) return MAGMA_ERR_DEVICE_ALLOC;
+        q->work_bytes = 64;
+    }
+    stats = (int *)q->work;
+    cudaMemsetAsync(stats, 0, 8 * sizeof(int), q->stream);
+    vb_check_kernel<<<(batch + 255) / 256, 256, 0, q->stream>>>(m, n, nrhs, ldda, lddb, batch, stats);
+    cudaMemcpyAsync(out, stats, 8 * sizeof(int), cudaMemcpyDeviceToHost, q->stream);
+    if (cudaStreamSynchronize(q->stream) != cudaSuccess) return MAGMA_ERR_UNKNOWN;
+    return 0;
+}
+
+// Workspace for vb_run owned by the queue (placed after the 64-byte stats area).
+static void *vb_queue_work(magma_queue_t q, int batch)
+{
+    const size_t need = 256 + vb_work_bytes(batch);
+    if (q->work_bytes < need) {
+        if (q->work) { cudaStreamSynchronize(q->stream); cudaFree(q->work); }
+        q->work = nullptr;
+        q->work_bytes = 0;
+        if (cudaMalloc(&q->work, need) != cudaSuccess) return nullptr;
+        q->work_bytes = need;
+    }
+    return (char *)q->work + 256;
+}
+
+}  // namespace mlu
+
+using namespace mlu;
+
+// ---------------------------------------------------------------------------
+// getrf
+
+template <typename T>
+static magma_int_t getrf_vbatched(const char *name, magma_int_t *m, magma_int_t *n, T **dA_array,
+                                  magma_int_t *ldda, magma_int_t **ipiv_array,
+                                  magma_int_t *info_array, magma_int_t batchCount,
+                                  magma_queue_t queue)
+{
+    int st[8];
+    magma_int_t rc = vb_check(m, n, nullptr, ldda, nullptr, batchCount, queue, st);
+    if (rc != 0) return rc;
+    magma_int_t arginfo = st[0] ? -1 : st[1] ? -2 : st[2] ? -4 : 0;
+    if (arginfo != 0) {
+        magma_xerbla(name, -arginfo);
+        return arginfo;
+    }
+    if (batchCount <= 0) return 0;
+    void *work = vb_queue_work(queue, batchCount);
+    if (!work) return MAGMA_ERR_DEVICE_ALLOC;
+    return vb_run<T>(m, n, nullptr, st[4], st[5], 0, dA_array, ldda, ipiv_array, nullptr, nullptr,
+                     info_array, work, batchCount, queue);
+}
+
+extern "C" magma_int_t magma_dgetrf_vbatched(magma_int_t *m, magma_int_t *n, double **dA_array,
+                                             magma_int_t *ldda, magma_int_t **ipiv_array,
+                                             magma_int_t *info_array, magma_int_t batchCount,
+                                             magma_queue_t queue)
+{
+    return getrf_vbatched<double>(__func__, m, n, dA_array, ldda, ipiv_array, info_array,
+                                  batchCount, queue);
+}
+
+extern "C" magma_int_t magma_sgetrf_vbatched(magma_int_t *m, magma_int_t *n, float **dA_array,
+                                             magma_int_t *ldda, magma_int_t **ipiv_array,
+                                             magma_int_t *info_array, magma_int_t batchCount,
+                                             magma_queue_t queue)
+{
+    return getrf_vbatched<float>(__func__, m, n, dA_array, ldda, ipiv_array, info_array,
+                                 batchCount, queue);
+}
+
+extern "C" magma_int_t
+magma_dgetrf_vbatched_max_nocheck_work(magma_int_t *m, magma_int_t *n, magma_int_t max_m,
+                                       magma_int_t max_n, magma_int_t max_minmn,
+                                       magma_int_t max_mxn, double **dA_array, magma_int_t *ldda,
+                                       magma_int_t **dipiv_array, magma_int_t *info_array,
+                                       void *work, magma_int_t *lwork, magma_int_t batchCount,
+                                       magma_queue_t queue)
+{
+    (void)max_minmn;
+    (void)max_mxn;
+    const size_t need = vb_work_bytes(mlu_max(batchCount, 0));
+    if (*lwork < 0) {
+        *lwork = (magma_int_t)need;
+        return 0;
+    }
+    if ((size_t)*lwork < need) return -12;
+    return vb_run<double>(m, n, nullptr, max_m, max_n, 0, dA_array, ldda, dipiv_array, nullptr,
+                          nullptr, info_array, work, batchCount, queue);
+}
+
+// ---------------------------------------------------------------------------
+// gesv / getrs (no counterpart in the reference)
+
+template <typename T>
+static magma_int_t gesv_vbatched(const char *name, magma_int_t *n, magma_int_t *nrhs, T **dA_array,
+                                 magma_int_t *ldda, magma_int_t **dipiv_array, T **dB_array,
+                                 magma_int_t *lddb, magma_int_t *dinfo_array,
+                                 magma_int_t batchCount, magma_queue_t queue)
+{
+    int st[8];
+    magma_int_t rc = vb_check(n, n, nrhs, ldda, lddb, batchCount, queue, st);
+    if (rc != 0) return rc;
+    magma_int_t arginfo = st[1] ? -1 : st[7] ? -2 : st[2] ? -4 : st[3] ? -7 : 0;
+    if (arginfo != 0) {
+        magma_xerbla(name, -arginfo);
+        return arginfo;
+    }
+    if (batchCount <= 0) return 0;
+    void *work = vb_queue_work(queue, batchCount);
+    if (!work) return MAGMA_ERR_DEVICE_ALLOC;
+    return vb_run<T>(n, n, nrhs, st[5], st[5], st[6], dA_array, ldda, dipiv_array, dB_array, lddb,
+                     dinfo_array, work, batchCount, queue);
+}
+
+extern "C" magma_int_t magma_dgesv_vbatched(magma_int_t *n, magma_int_t *nrhs, double **dA_array,
+                                            magma_int_t *ldda, magma_int_t **dipiv_array,
+                                            double **dB_array, magma_int_t *lddb,
+                                            magma_int_t *dinfo_array, magma_int_t batchCount,
+                                            magma_queue_t queue)
+{
+    return gesv_vbatched<double>(__func__, n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb,
+                                 dinfo_array, batchCount, queue);
+}
+
+extern "C" magma_int_t magma_sgesv_vbatched(magma_int_t *n, magma_int_t *nrhs, float **dA_array,
+                                            magma_int_t *ldda, magma_int_t **dipiv_array,
+                                            float **dB_array, magma_int_t *lddb,
+                                            magma_int_t *dinfo_array, magma_int_t batchCount,
+                                            magma_queue_t queue)
+{
+    return gesv_vbatched<float>(__func__, n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb,
+                                dinfo_array, batchCount, queue);
+}
+
+extern "C" magma_int_t
+magma_dgesv_vbatched_max_nocheck_work(magma_int_t *n, magma_int_t *nrhs, magma_int_t max_n,
+                                      magma_int_t max_nrhs, double **dA_array, magma_int_t *ldda,
+                                      magma_int_t **dipiv_array, double **dB_array,
+                                      magma_int_t *lddb, magma_int_t *dinfo_array, void *work,
+                                      magma_int_t *lwork, magma_int_t batchCount,
+                                      magma_queue_t queue)
+{
+    const size_t need = vb_work_bytes(mlu_max(batchCount, 0));
+    if (*lwork < 0) {
+        *lwork = (magma_int_t)need;
+        return 0;
+    }
+    if ((size_t)*lwork < need) return -12;
+    return vb_run<double>(n, n, nrhs, max_n, max_n, max_nrhs, dA_array, ldda, dipiv_array,
+                          dB_array, lddb, dinfo_array, work, batchCount, queue);
+}
+
+template <typename T>
+static magma_int_t getrs_vbatched(const char *name, magma_trans_t trans, magma_int_t *n,
+                                  magma_int_t *nrhs, T **dA_array, magma_int_t *ldda,
+                                  magma_int_t **dipiv_array, T **dB_array, magma_int_t *lddb,
+                                  magma_int_t batchCount, magma_queue_t queue)
+{
+    if (trans != MagmaNoTrans && trans != MagmaTrans && trans != MagmaConjTrans) {
+        magma_xerbla(name, 1);
+        return -1;
+    }
+    int st[8];
+    magma_int_t rc = vb_check(n, n, nrhs, ldda, lddb, batchCount, queue, st);
+    if (rc != 0) return rc;
+    magma_int_t arginfo = st[1] ? -2 : st[7] ? -3 : st[2] ? -5 : st[3] ? -8 : 0;
+    if (arginfo != 0) {
+        magma_xerbla(name, -arginfo);
+        return arginfo;
+    }
+    return vb_getrs_run<T>(trans != MagmaNoTrans, n, nrhs, st[5], st[6], dA_array, ldda, dipiv_array,
+                           dB_array, lddb, batchCount, queue);
+}
+
+extern "C" magma_int_t magma_dgetrs_vbatched(magma_trans_t trans, magma_int_t *n,
+                                             magma_int_t *nrhs, double **dA_array,
+                                             magma_int_t *ldda, magma_int_t **dipiv_array,
+                                             double **dB_array, magma_int_t *lddb,
+                                             magma_int_t batchCount, magma_queue_t queue)
+{
+    return getrs_vbatched<double>(__func__, trans, n, nrhs, dA_array, ldda, dipiv_array, dB_array,
+                                  lddb, batchCount, queue);
+}
+
+extern "C" magma_int_t magma_sgetrs_vbatched(magma_trans_t trans, magma_int_t *n,
+                                             magma_int_t *nrhs, float **dA_array,
+                                             magma_int_t *ldda, magma_int_t **dipiv_array,
+                                             float **dB_array, magma_int_t *lddb,
+                                             magma_int_t batchCount, magma_queue_t queue)
+{
+    return getrs_vbatched<float>(__func__, trans, n, nrhs, dA_array, ldda, dipiv_array, dB_array,
+                                 lddb, batchCount, queue);
+}

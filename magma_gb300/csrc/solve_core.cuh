@@ -7,18 +7,35 @@
 // then updated by all threads; every element receives its updates in the
 // order of the CPU oracle (oracle/lu_oracle.c, getrs), so results are
 // bit-identical to it.  Must be called by all threads of the block; ends with
-// a __syncthreads.
+// a __syncthreads.  ipiv == nullptr skips the row interchanges (the caller
+// has applied them already).
 #pragma once
 #include "common.cuh"
 
 namespace mlu {
 
+// Warp-level copy of the tb x tb diagonal block at (t0, t0) into sD[r][c]
+// (coalesced: lanes run down a column), so that the sequential block solves
+// below read shared memory instead of issuing one dependent global load per
+// step.  Ends with __syncwarp.
+template <typename T>
+__device__ __forceinline__ void stage_diag_block(const T *A, int ldda, int t0, int tb,
+                                                 T (*sD)[33])
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll 8
+    for (int c = 0; c < 32; c++)
+        if (c < tb && lane < tb) sD[lane][c] = A[t0 + lane + (size_t)(t0 + c) * ldda];
+    __syncwarp();
+}
+
 template <typename T, bool TRANS, int SOLVE_NR>
 __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, int nr)
 {
+    __shared__ T sD[32][33];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (!TRANS) {
-        if (tid < nr) {
+        if (ipiv != nullptr && tid < nr) {
             T *b = sB + tid * n;
             for (int k = 0; k < n; k++) {
                 const int p = ipiv[k] - 1;
@@ -32,11 +49,11 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
             if (warp == 0) {
                 T y[SOLVE_NR];
                 const bool v = lane < tb;
-                const T *Lc = A + t0 + lane;   // row t0+lane
+                stage_diag_block<T>(A, ldda, t0, tb, sD);
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
                 for (int t = 0; t < tb; t++) {
-                    const T l = v ? Lc[(size_t)(t0 + t) * ldda] : T(0);
+                    const T l = v ? sD[lane][t] : T(0);   // L(t0+lane, t0+t)
 #pragma unroll
                     for (int c = 0; c < SOLVE_NR; c++) {
                         const T yt = __shfl_sync(FULL, y[c], t);
@@ -68,11 +85,11 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
             if (warp == 0) {
                 T y[SOLVE_NR];
                 const bool v = lane < tb;
-                const T *Ur = A + t0 + lane;
+                stage_diag_block<T>(A, ldda, t0, tb, sD);
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
                 for (int t = tb - 1; t >= 0; t--) {
-                    const T u = v ? Ur[(size_t)(t0 + t) * ldda] : T(0);   // U(t0+lane, t0+t)
+                    const T u = v ? sD[lane][t] : T(0);   // U(t0+lane, t0+t)
                     const T d = __shfl_sync(FULL, u, t);
                     const T r = T(1) / d;
 #pragma unroll
@@ -108,11 +125,11 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
             if (warp == 0) {
                 T y[SOLVE_NR];
                 const bool v = lane < tb;
-                const T *Ucol = A + (size_t)(t0 + lane) * ldda;   // column t0+lane
+                stage_diag_block<T>(A, ldda, t0, tb, sD);
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
                 for (int t = 0; t < tb; t++) {
-                    const T u = v ? Ucol[t0 + t] : T(0);          // U(t0+t, t0+lane)
+                    const T u = v ? sD[t][lane] : T(0);           // U(t0+t, t0+lane)
                     const T d = __shfl_sync(FULL, u, t);
                     const T r = T(1) / d;
 #pragma unroll
@@ -148,11 +165,11 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
             if (warp == 0) {
                 T y[SOLVE_NR];
                 const bool v = lane < tb;
-                const T *Lcol = A + (size_t)(t0 + lane) * ldda;
+                stage_diag_block<T>(A, ldda, t0, tb, sD);
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
                 for (int t = tb - 1; t >= 0; t--) {
-                    const T l = v ? Lcol[t0 + t] : T(0);          // L(t0+t, t0+lane)
+                    const T l = v ? sD[t][lane] : T(0);           // L(t0+t, t0+lane)
 #pragma unroll
                     for (int c = 0; c < SOLVE_NR; c++) {
                         const T x = __shfl_sync(FULL, y[c], t);
@@ -179,7 +196,7 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
             }
             __syncthreads();
         }
-        if (tid < nr) {
+        if (ipiv != nullptr && tid < nr) {
             T *b = sB + tid * n;
             for (int k = n - 1; k >= 0; k--) {
                 const int p = ipiv[k] - 1;

@@ -49,6 +49,29 @@ for _p in "ds":
     _PROTOS[f"magma_{_p}getrs_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_int, c_ptr], c_int)
     _PROTOS[f"magma_{_p}gesv_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr, c_int, c_ptr], c_int)
     _PROTOS[f"magma_{_p}gesv_batched_small"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr, c_int, c_ptr], c_int)
+for _p in "ds":
+    _PROTOS[f"magma_{_p}getrf_vbatched"] = ([c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}getrs_vbatched"] = ([c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                                            c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}gesv_vbatched"] = ([c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                                           c_int, c_ptr], c_int)
+_PROTOS["magma_dgetrf_vbatched_max_nocheck_work"] = (
+    [c_ptr, c_ptr, c_int, c_int, c_int, c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+     C.POINTER(c_int), c_int, c_ptr], c_int)
+_PROTOS["magma_dgesv_vbatched_max_nocheck_work"] = (
+    [c_ptr, c_ptr, c_int, c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+     C.POINTER(c_int), c_int, c_ptr], c_int)
+for _p in "ds":
+    _PROTOS[f"magma_{_p}gesv_adjoint_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int,
+                                                  c_ptr, c_int, c_ptr, c_int, c_int, c_ptr], c_int)
+    _PROTOS[f"magmablas_{_p}ger_neg_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr,
+                                                 c_int, c_int, c_ptr], c_int)
+_PROTOS["magma_sgetrf_batched_tc"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_ptr,
+                                       C.POINTER(C.c_size_t), c_int, c_ptr], c_int)
+_PROTOS["magma_sgetrf_batched_tc_status"] = ([c_int, c_int, c_ptr, c_int, c_ptr], c_int)
+_PROTOS["magma_dxgesv_batched_work"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int,
+                                         c_ptr, c_int, c_ptr, c_ptr, c_int, C.c_double, c_int,
+                                         c_ptr, C.POINTER(C.c_size_t), c_int, c_ptr], c_int)
 _PROTOS["magma_dsgesv_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr, c_int,
                                    c_ptr, c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_dsgesv_batched_noalloc"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr,

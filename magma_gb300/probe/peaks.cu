@@ -56,3 +56,61 @@ extern "C" double mlu_probe_fp64_tflops(void *stream) {
 extern "C" double mlu_probe_fp32_tflops(void *stream) {
     return run<float>(16384, 4, 256, (cudaStream_t)stream);
 }
+
+// ---------------------------------------------------------------------------
+// Check of the integer-pipe double -> float conversion used by the refinement
+// (csrc/convert.cuh) against CUDA's __double2float_rn: random 64-bit patterns
+// and doubles built around float rounding boundaries (random low bits, exact
+// ties, ties +- 1 ulp of double).  Returns the number of mismatching results
+// (NaN matches any NaN).
+#include "../csrc/convert.cuh"
+
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x)
+{
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+__global__ void d2f_check_kernel(unsigned long long seed, long long n, unsigned long long *bad)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long r = splitmix64(seed ^ (unsigned long long)i);
+        unsigned long long bits;
+        const int mode = (int)(i & 3);
+        if (mode == 0) {
+            bits = r;
+        } else {
+            // a double whose top part is a random float, exponent biased to the
+            // float range (including its subnormals), with chosen low bits
+            const unsigned long long r2 = splitmix64(r);
+            const int e = 1023 - 160 + (int)(r2 % 300);      // 2^-160 .. 2^139
+            const unsigned long long top = (r >> 11) & 0xfffffffffffffull;
+            unsigned long long low;
+            if (mode == 1) low = (r2 >> 20) & ((1ull << 29) - 1);
+            else if (mode == 2) low = 1ull << 28;                       // exact tie
+            else low = (1ull << 28) + ((r2 & 1) ? 1 : (1ull << 29) - 1) - ((r2 & 1) ? 0 : (1ull << 28));
+            bits = ((r >> 63) << 63) | ((unsigned long long)e << 52) | ((top & ~((1ull << 29) - 1)) | low);
+        }
+        const double x = __longlong_as_double((long long)bits);
+        const float a = __double2float_rn(x);
+        const float b = mlu::d2f_rn_int(x);
+        const bool both_nan = (a != a) && (b != b);
+        if (!both_nan && __float_as_uint(a) != __float_as_uint(b)) atomicAdd(bad, 1ull);
+    }
+}
+
+extern "C" long long mlu_check_d2f(long long n, unsigned long long seed)
+{
+    unsigned long long *bad = nullptr;
+    if (cudaMalloc(&bad, sizeof(unsigned long long)) != cudaSuccess) return -1;
+    cudaMemset(bad, 0, sizeof(unsigned long long));
+    d2f_check_kernel<<<1024, 256>>>(seed, n, bad);
+    unsigned long long h = 0;
+    cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    if (cudaGetLastError() != cudaSuccess) return -1;
+    return (long long)h;
+}

@@ -202,7 +202,8 @@ int oracle_max_threads(void)
 /* Batched mixed-precision iterative refinement, one matrix: the restatement of
  * magma_dsgesv_gpu (src/zcgesv_gpu.cpp:144-366) in the exact arithmetic order
  * of the GPU implementation:
- *   anrm = max_i sum_j |a_ij| (j ascending); As = (float)A (overflow: iter -2);
+ *   anrm = max_i of the FP32 sum over j ascending of |(float)a_ij|; As = (float)A
+ *   (overflow: iter -2);
  *   sgetrf(As) (info > 0: iter -3); X = 0, R = B;
  *   solve: X = X + (double)sgetrs(As, (float)R);
  *   residual: r_i = b_i, r_i = fma(-a_ij, x_j, r_i) for j ascending;
@@ -223,15 +224,15 @@ int oracle_dsgesv(int n, int nrhs, double *A, int lda, const double *B, int ldb,
     float *Rs = (float *)malloc(sizeof(float) * (size_t)n * nrhs + 4);
     double *R = (double *)malloc(sizeof(double) * (size_t)n * nrhs + 8);
     for (int i = 0; i < n; i++) {
-        double rs = 0.0;
+        float rs = 0.0f;             /* FP32 row sums of |float(a_ij)|, j ascending */
         for (int j = 0; j < n; j++) {
             double a = A[i + (size_t)j * lda];
-            rs += fabs(a);
             float f = (float)a;
+            rs += fabsf(f);
             if (isinf(f) && !isinf(a)) ovf = 1;
             As[i + (size_t)j * n] = f;
         }
-        if (rs > anrm) anrm = rs;
+        if ((double)rs > anrm) anrm = (double)rs;
     }
     int iter = 0, info = 0, state = 0;   /* 0 active, 1 converged, 2 failed */
     if (ovf) { iter = -2; state = 2; }
@@ -306,3 +307,33 @@ void oracle_dsgesv_batched(int n, int nrhs, double *A, int lda, long strideA, co
                                 X + k * strideX, ldx, ipiv + k * strideP, itermax, tol, fallback,
                                 iter + k);
 }
+
+/* Adjoint of x = A^{-1} b with the forward LU kept: G <- A^{-T} G (getrs with
+ * TRANS='T'), then GA(i,j) = -(sum_c G(i,c) X(j,c)) accumulated as
+ * acc = fma(G(i,c), X(j,c), acc) for c ascending from acc = 0. */
+#define DEFINE_ADJOINT(T, P, FMA)                                                          \
+void oracle_##P##gesv_adjoint(int n, int nrhs, const T *LU, int lda, const int *ipiv,    \
+                              const T *X, int ldx, T *G, int ldg, T *GA, int ldga)       \
+{                                                                                        \
+    oracle_##P##getrs(1, n, nrhs, LU, lda, ipiv, G, ldg);                                \
+    for (int j = 0; j < n; j++)                                                          \
+        for (int i = 0; i < n; i++) {                                                    \
+            T acc = (T)0;                                                                \
+            for (int c = 0; c < nrhs; c++)                                               \
+                acc = FMA(G[i + (size_t)c * ldg], X[j + (size_t)c * ldx], acc);          \
+            GA[i + (size_t)j * ldga] = -acc;                                             \
+        }                                                                                \
+}                                                                                        \
+void oracle_##P##gesv_adjoint_batched(int n, int nrhs, const T *LU, int lda, long sLU,   \
+                                      const int *ipiv, long sP, const T *X, int ldx,     \
+                                      long sX, T *G, int ldg, long sG, T *GA, int ldga,  \
+                                      long sGA, int batch, int nthreads)                 \
+{                                                                                        \
+    (void)nthreads;                                                                      \
+    _Pragma("omp parallel for schedule(dynamic) num_threads(nthreads)")                 \
+    for (int k = 0; k < batch; k++)                                                      \
+        oracle_##P##gesv_adjoint(n, nrhs, LU + k * sLU, lda, ipiv + k * sP, X + k * sX,  \
+                                 ldx, G + k * sG, ldg, GA + k * sGA, ldga);              \
+}
+DEFINE_ADJOINT(double, d, fma)
+DEFINE_ADJOINT(float, s, fmaf)

@@ -201,3 +201,22 @@ def dsgesv_batched(A, B, itermax=30, tol=0.0, fallback=True, nthreads=None):
        ipiv.shape[1], _p(info), _p(iters), itermax, float(tol), 1 if fallback else 0, b,
        _threads(nthreads))
     return X, ipiv, info, iters
+
+
+def gesv_adjoint_batched(LU, ipiv, X, G, nthreads=None):
+    """G <- A^{-T} G and returns GA = -G X^T (storage layout), the oracle's
+    restatement of the adjoint.  LU (batch, n, ld), X and G (batch, nrhs, ld)."""
+    lib = load()
+    pre = "d" if LU.dtype == np.float64 else "s"
+    b, n, ld = LU.shape
+    nrhs, ldx = X.shape[1], X.shape[2]
+    ldg = G.shape[2]
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    GA = np.zeros((b, n, n), dtype=LU.dtype)
+    fn = getattr(lib, f"oracle_{pre}gesv_adjoint_batched")
+    fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_long,
+                   C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_int, C.c_long, C.c_void_p,
+                   C.c_int, C.c_long, C.c_int, C.c_int]
+    fn(n, nrhs, _p(LU), ld, n * ld, _p(ipiv), ipiv.shape[1], _p(X), ldx, nrhs * ldx, _p(G), ldg,
+       nrhs * ldg, _p(GA), n, n * n, b, _threads(nthreads))
+    return GA

@@ -127,3 +127,29 @@ def test_dsgesv_public_entry_uses_queue_workspace(cuda):
     assert rc == 0
     assert np.array_equal(dX.cpu().numpy(), rX)
     assert np.array_equal(iters.cpu().numpy(), riters)
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp16"])
+def test_dxgesv_tensor_core_factorisation(cuda, precision):
+    """FP32 factorisation with tensor-core (BF16 / FP16) trailing updates + FP64
+    refinement: every solve ends FP64-accurate; the well-conditioned third
+    converges by refinement alone."""
+    n, nrhs = 320, 4
+    A = _svd(6, n, [1e2, 1e2, 1e4, 1e4, 1e6, 1e6], seed=21)
+    Bm = np.random.default_rng(21).uniform(-1, 1, (6, n, nrhs))
+    dS = torch.from_numpy(to_storage(A)).to(cuda)
+    dB = torch.from_numpy(to_storage(Bm)).to(cuda)
+    X, ipiv, info, iters = mg.dsgesv_batched(dS, dB, tol=30.0, precision=precision)
+    torch.cuda.synchronize()
+    it = iters.cpu().numpy()
+    assert np.all(it[:2] >= 0), it
+    res = scaled_residual(A, from_storage(X.cpu().numpy(), n), Bm)
+    assert res.max() <= 30, (res, it)
+
+
+def test_dxgesv_fp32_equals_dsgesv(cuda):
+    """Precision 900 of the general entry is the FP32 refinement, bit for bit."""
+    A = _svd(3, 100, [1e3] * 3, seed=8)
+    Bm = np.random.default_rng(8).uniform(-1, 1, (3, 100, 2))
+    gpu, ref = _run_both(A, Bm, cuda)
+    _assert_same(gpu, ref, 100)
