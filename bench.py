@@ -124,7 +124,7 @@ class Gesv32:
         if rc != 0:
             raise RuntimeError(f"magma_dgesv_batched returned {rc}")
 
-    kernels_per_step = 1
+    dominant_class = "small_gesv"
     dominant = "mlu::small_gesv_kernel<double,32,1>"
 
     def e2e_setup(self, c):
@@ -155,19 +155,20 @@ class Gesv32:
     def flops_per_solve(self):
         return flops_getrf(self.n, self.n) + flops_getrs(self.n, self.nrhs)
 
-    def roofline(self, step_ms, peaks):
-        flops = self.flops_per_solve() * self.batch
+    def roofline(self, kern, peaks, c):
+        flops = self.flops_per_solve() * self.batch          # one launch per step
         n, r = self.n, self.nrhs
         nbytes = (16 * n * n + 16 * n * r + 4 * n + 4 + 24) * self.batch
-        ach = flops / (step_ms * 1e-3) / 1e12
+        ms = kern["launch_ms"]
+        ach = flops / (ms * 1e-3) / 1e12
         return {"bound": "fp64", "achieved": ach, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
                 "frac": ach / peaks["fp64_tflops"], "traffic": _traffic(self.name),
                 "peak_source": "FP64 FMA-throughput probe run inside bench.py "
                                "(magma_gb300/probe/peaks.cu)",
-                "kernel": self.dominant, "launch_ms": step_ms,
-                "algorithmic_flops_per_launch": flops, "algorithmic_bytes_per_launch": nbytes,
-                "hbm_gbs": nbytes / (step_ms * 1e-3) / 1e9,
-                "hbm_frac_of_measured": nbytes / (step_ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+                **kern, "algorithmic_flops_per_launch": flops,
+                "algorithmic_bytes_per_launch": nbytes,
+                "hbm_gbs": nbytes / (ms * 1e-3) / 1e9,
+                "hbm_frac_of_measured": nbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
 
     def cpu_sample(self, nthreads, target_s):
         import oracle
@@ -242,8 +243,8 @@ class Dsgesv512:
         if rc != 0:
             raise RuntimeError(f"magma_dsgesv_batched_work returned {rc}")
 
-    kernels_per_step = None   # set after a run from the launch list
-    dominant = "ir_residual_kernel<4> (FP64 residual)"
+    dominant_class = "ir_residual"
+    dominant = "mlu::ir_residual_kernel<4> (FP64 residual R = B - A X)"
 
     def e2e_setup(self, c):
         import torch
@@ -308,9 +309,32 @@ class Dsgesv512:
                 "max_scaled_residual": float(res.max()), "steps": steps,
                 "call": "magma_dgesv_batched"}
 
-    def roofline(self, step_ms, peaks, phase_ms=None):
-        # dominant kernel: FP64 residual R = B - A X (n*n*nrhs FMA per matrix per pass)
-        return None
+    def passes(self, c):
+        """Residual passes per matrix in the last step: the initial residual plus one per
+        iteration (itermax + 1 for a matrix that did not converge)."""
+        it = c["iter"].cpu().numpy()
+        return np.where(it >= 0, it + 1, self.itermax + 1)
+
+    def roofline(self, kern, peaks, c):
+        n, r, b = self.n, self.nrhs, self.batch
+        ms_step = kern["ms"] / kern["steps"]
+        if self.dominant_class == "ir_residual":
+            # 2 n^2 r FP64 flops per matrix and pass; A read once per pass (FP64)
+            passes = int(self.passes(c).sum())
+            flops = 2.0 * n * n * r * passes
+            nbytes = (8.0 * n * n + 3 * 8.0 * n * r) * passes
+            peak, unit, bound = peaks["fp64_tflops"], "TFLOP/s", "fp64"
+            src = "FP64 FMA-throughput probe run inside bench.py (magma_gb300/probe/peaks.cu)"
+            ach = flops / (ms_step * 1e-3) / 1e12
+            extra = {"residual_passes_per_step": passes}
+        else:
+            raise ValueError(self.dominant_class)
+        return {"bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
+                "traffic": _traffic(self.name), "peak_source": src, **kern,
+                "algorithmic_flops_per_step": flops, "algorithmic_bytes_per_step": nbytes,
+                "hbm_gbs": nbytes / (ms_step * 1e-3) / 1e9,
+                "hbm_frac_of_measured": nbytes / (ms_step * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                **extra}
 
     def cpu_sample(self, nthreads, target_s):
         import oracle
@@ -419,7 +443,8 @@ class GesvVbatched:
     def step(self, c, i):
         c["graphs"][i].replay()
 
-    kernels_per_step = 2
+    dominant_class = None        # graph replay: the step is the sort + the persistent kernel
+    graph_kernels_per_step = 2
     dominant = "mlu::vb_lu_kernel<double> (persistent)"
 
     def e2e_setup(self, c):
@@ -451,14 +476,16 @@ class GesvVbatched:
             ok += r <= 30
         return ok, worst
 
-    def roofline(self, step_ms, peaks):
+    def roofline(self, kern, peaks, c):
         flops = self.flops_total()
-        ach = flops / (step_ms * 1e-3) / 1e12
+        ms = kern["launch_ms"]
+        ach = flops / (ms * 1e-3) / 1e12
         return {"bound": "fp64", "achieved": ach, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
                 "frac": ach / peaks["fp64_tflops"], "traffic": _traffic(self.name),
                 "peak_source": "FP64 FMA-throughput probe run inside bench.py",
-                "kernel": self.dominant, "launch_ms": step_ms,
-                "algorithmic_flops_per_launch": flops}
+                **kern, "algorithmic_flops_per_launch": flops,
+                "note": "timed as the CUDA-graph replay (size sort + persistent kernel); the "
+                        "sort's share of the replay is in the launch-list summary"}
 
     def cpu_sample(self, nthreads, target_s):
         import oracle
@@ -514,8 +541,8 @@ class Adjoint2048:
         X.backward(c["gX"])
         c["last_X"] = X
 
-    kernels_per_step = None
-    dominant = "forward small-n LU (blocked path, n=64) + adjoint"
+    dominant_class = "getrs"
+    dominant = "triangular solves (forward getrs and transposed adjoint getrs)"
 
     def e2e_setup(self, c):
         import torch
@@ -550,15 +577,18 @@ class Adjoint2048:
         res = scaled_residuals(c["A0"], c["last_X"].detach(), c["B0"])
         return int((res <= 30).sum()), float(res.max()), {"grad_rel_err_vs_torch_fp64": rel}
 
-    def roofline(self, step_ms, peaks):
+    def roofline(self, kern, peaks, c):
+        # two triangular-solve launches per step (forward solve, transposed solve)
         b, n, r = self.batch, self.n, self.nrhs
-        flops = b * (flops_getrf(n, n) + flops_getrs(n, r) + flops_getrs(n, r) + 2.0 * n * n * r)
-        ach = flops / (step_ms * 1e-3) / 1e12
-        return {"bound": "fp64", "achieved": ach, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
-                "frac": ach / peaks["fp64_tflops"], "traffic": None,
-                "peak_source": "FP64 FMA-throughput probe run inside bench.py",
-                "kernel": self.dominant, "launch_ms": step_ms,
-                "algorithmic_flops_per_launch": flops}
+        flops = b * 2 * flops_getrs(n, r)
+        nbytes = b * 2 * (8.0 * n * n + 2 * 8.0 * n * r + 4 * n)
+        ms_step = kern["ms"] / kern["steps"]
+        ach = nbytes / (ms_step * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / peaks["hbm_gbs"], "traffic": _traffic(self.name),
+                "peak_source": peaks["hbm_source"], **kern,
+                "algorithmic_bytes_per_step": nbytes, "algorithmic_flops_per_step": flops,
+                "fp64_tflops": flops / (ms_step * 1e-3) / 1e12}
 
     def cpu_sample(self, nthreads, target_s):
         import oracle
@@ -650,6 +680,35 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+class KernelTimer:
+    """CUDA-event timing of one kernel class inside the library (magma_lu_timing_start /
+    magma_lu_timing_stop): events on the launching stream around each launch."""
+
+    def __init__(self, lib, cls):
+        from magma_gb300.lib import KERNEL_CLASSES
+        self.lib = lib
+        self.cls = cls
+        self.id = KERNEL_CLASSES[cls] if cls else None
+
+    def start(self):
+        if self.id is not None:
+            rc = self.lib.magma_lu_timing_start(self.id, 1 << 16)
+            if rc != 0:
+                raise RuntimeError(f"magma_lu_timing_start returned {rc}")
+
+    def stop(self, steps):
+        if self.id is None:
+            return None
+        n, dropped, ms = C.c_int(0), C.c_int(0), C.c_double(0)
+        rc = self.lib.magma_lu_timing_stop(C.byref(n), C.byref(dropped), C.byref(ms))
+        if rc != 0 or n.value == 0:
+            raise RuntimeError(f"magma_lu_timing_stop returned {rc}, {n.value} launches")
+        return {"kernel_class": self.cls, "launches": n.value, "dropped": dropped.value,
+                "steps": steps, "ms": ms.value, "launch_ms": ms.value / n.value,
+                "timing": "CUDA events on the launching stream around every launch of the "
+                          "class inside the timed region"}
 
 
 def dist_setup():
@@ -777,6 +836,9 @@ def run_ours(args, wl):
           for _ in range(args.steps)]
     barrier(pg, dev)
     torch.cuda.synchronize(dev)
+    tracer = KernelTimer(lib, wl.dominant_class)
+    tracer.start()
+    n_launch0 = lib.magma_lu_launch_count()
     clocks.start()
     time.sleep(0.3)
     start = torch.cuda.Event(enable_timing=True)
@@ -790,6 +852,9 @@ def run_ours(args, wl):
     torch.cuda.synchronize(dev)
     barrier(pg, dev)
     clk = clocks.stop()
+    launches = lib.magma_lu_launch_count() - n_launch0 + \
+        getattr(wl, "graph_kernels_per_step", 0) * args.steps
+    kern = tracer.stop(args.steps)
     ms = allmax(pg, start.elapsed_time(end), dev)
     step_ms = statistics.mean(e0.elapsed_time(e1) for e0, e1 in ev)
     ms_per_step = ms / args.steps
@@ -819,7 +884,11 @@ def run_ours(args, wl):
     if rank != 0:
         return 0
     cpu = cpu_baseline(wl) if world == 1 else None
-    roof = wl.roofline(step_ms, peaks)
+    if kern is None:
+        kern = {"kernel_class": None, "launches": args.steps, "steps": args.steps,
+                "ms": step_ms * args.steps, "launch_ms": step_ms}
+    kern["kernel"] = wl.dominant
+    roof = wl.roofline(kern, peaks, c)
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -829,7 +898,7 @@ def run_ours(args, wl):
         "cpu_baseline": cpu,
         "e2e": {"value": world * wl.batch / (e2e_ms * 1e-3), "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "gpu_launches": (wl.kernels_per_step * args.steps) if wl.kernels_per_step else None,
+        "gpu_launches": launches,
         "clocks": clk,
         "accuracy": {"max_scaled_residual": max_res, "solves_within_30": n_ok, "of": wl.batch,
                      **extra},

@@ -435,6 +435,30 @@ magma_int_t magma_dxgesv_batched_work(magma_int_t precision, magma_int_t n, magm
                                       void *work, size_t *lwork,
                                       magma_int_t batchCount, magma_queue_t queue);
 
+/* ------------------------------------------------------------------------
+ * Launch accounting and kernel timing.  No counterpart in the reference,
+ * whose testers time whole calls on the host
+ * (testing/testing_zgesv_batched.cpp:158-166).
+ *
+ * magma_lu_launch_count: number of kernels this library has launched in the
+ * process (graph capture counts the captured launches once).
+ *
+ * magma_lu_timing_start: from now on every launch of one kernel class, on any
+ * queue and outside stream capture, is bracketed by CUDA events on its stream,
+ * for up to `capacity` launches (later ones are counted as dropped).  Classes:
+ * 1 fused n<=32 factor+solve, 2 panel, 3 interchanges + L11^{-1}A12, 4 SIMT
+ * trailing update, 5 tensor-core trailing update, 6 triangular solves,
+ * 7 refinement FP64 residual, 8 refinement correction solve, 9 refinement
+ * conversion, 10 variable-size persistent factor+solve, 11 adjoint outer
+ * product.  Returns -1 for a bad class, -2 for a bad capacity.
+ *
+ * magma_lu_timing_stop: waits for the recorded events, returns the number of
+ * timed launches, the number dropped and their summed device time, and turns
+ * timing off.  Use from one host thread. */
+long long magma_lu_launch_count(void);
+magma_int_t magma_lu_timing_start(magma_int_t kernel_class, magma_int_t capacity);
+magma_int_t magma_lu_timing_stop(magma_int_t *launches, magma_int_t *dropped, double *total_ms);
+
 #ifdef __cplusplus
 }
 #endif

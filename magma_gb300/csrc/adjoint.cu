@@ -11,6 +11,7 @@
 // block, acc = fma(gb_ic, x_jc, acc) for c ascending, gA_ij = -acc.  The
 // kernel is bound by the write of gA (8 n^2 bytes per matrix in FP64).
 #include "common.cuh"
+#include "trace.cuh"
 
 extern "C" magma_int_t magma_dgetrs_batched(magma_trans_t, magma_int_t, magma_int_t, double **,
                                             magma_int_t, magma_int_t **, double **, magma_int_t,
@@ -83,8 +84,8 @@ magma_int_t ger_neg(int n, int nrhs, T **dG, int lddg, T **dX, int lddx, T **dGA
     const int tiles = (n + GER_TILE - 1) / GER_TILE;
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
-        ger_neg_kernel<T><<<dim3(tiles * tiles, nb), 256, 0, q->stream>>>(
-            n, nrhs, dG + b0, lddg, dX + b0, lddx, dGA + b0, lddga, tiles);
+        MLU_LAUNCH(mlu::KC_ADJ_GER, q->stream, ger_neg_kernel<T><<<dim3(tiles * tiles, nb), 256, 0, q->stream>>>(
+            n, nrhs, dG + b0, lddg, dX + b0, lddx, dGA + b0, lddga, tiles));
     }
     MLU_CHECK_LAUNCH();
     return 0;

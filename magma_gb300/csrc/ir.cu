@@ -24,6 +24,7 @@
 // the FP64 residual, the oracle's order in the FP32 factor and solves), so the
 // CPU oracle reproduces iterates and iteration counts exactly.
 #include "common.cuh"
+#include "trace.cuh"
 #include "convert.cuh"
 #include "solve_core.cuh"
 
@@ -417,8 +418,8 @@ static void launch_residual(int n, int nrhs, double **dA, int ldda, double **dB,
     const size_t smem = (size_t)n * NR * sizeof(double);
     static size_t dyn_max = 0;
     if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(ir_residual_kernel<NR>);
-    ir_residual_kernel<NR><<<dim3((n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS, smem, s>>>(
-        n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par);
+    MLU_LAUNCH(mlu::KC_IR_RESIDUAL, s, ir_residual_kernel<NR><<<dim3((n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS, smem, s>>>(
+        n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par));
 }
 
 static void residual(int n, int nrhs, double **dA, int ldda, double **dB, int lddb, double **dX,
@@ -483,17 +484,17 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
     double *R = (double *)(w + L.r);
 
     cudaMemsetAsync(w, 0, L.asp, s);   // stats, counters
-    set_float_pointers<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(As_array, As,
-                                                                     (size_t)n * L.ldas, batchCount);
+    MLU_LAUNCH(mlu::KC_OTHER, s, set_float_pointers<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(As_array, As,
+                                                                     (size_t)n * L.ldas, batchCount));
     double *rsc = prec == 905 ? (double *)(w + L.rsc) : nullptr;
     double *csc = prec == 905 ? (double *)(w + L.csc) : nullptr;
     const dim3 rows_grid((n + IR_ROWS - 1) / IR_ROWS, batchCount);
-    ir_init_kernel<<<rows_grid, IR_ROWS, 0, s>>>(n, nrhs, dA_array, ldda, As_array, L.ldas,
+    MLU_LAUNCH(mlu::KC_IR_INIT, s, ir_init_kernel<<<rows_grid, IR_ROWS, 0, s>>>(n, nrhs, dA_array, ldda, As_array, L.ldas,
                                                  dB_array, lddb, dX_array, lddx, R, stats,
-                                                 diter_array, rsc);
+                                                 diter_array, rsc));
     if (rsc)
-        ir_colscale_kernel<<<dim3((n + 127) / 128, batchCount), 128, 0, s>>>(
-            n, dA_array, ldda, As_array, L.ldas, rsc, csc);
+        MLU_LAUNCH(mlu::KC_IR_INIT, s, ir_colscale_kernel<<<dim3((n + 127) / 128, batchCount), 128, 0, s>>>(
+            n, dA_array, ldda, As_array, L.ldas, rsc, csc));
     magma_int_t rc;
     if (prec == 900) {
         rc = magma_sgetrf_batched(n, n, As_array, L.ldas, dipiv_array, dinfo_array, batchCount,
@@ -510,13 +511,13 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
     auto solve = [&](int it) {
         const dim3 grid(mlu_ceildiv(nrhs, snr), batchCount);
         if (snr == 4)
-            ir_solve_kernel<4><<<grid, 256, ssmem, s>>>(n, nrhs, As_array, L.ldas, dipiv_array,
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4><<<grid, 256, ssmem, s>>>(n, nrhs, As_array, L.ldas, dipiv_array,
                                                         dX_array, lddx, R, stats, diter_array,
-                                                        dinfo_array, it, tol, rsc, csc);
+                                                        dinfo_array, it, tol, rsc, csc));
         else
-            ir_solve_kernel<IR_SOLVE_NR><<<grid, 256, ssmem, s>>>(
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<IR_SOLVE_NR><<<grid, 256, ssmem, s>>>(
                 n, nrhs, As_array, L.ldas, dipiv_array, dX_array, lddx, R, stats, diter_array,
-                dinfo_array, it, tol, rsc, csc);
+                dinfo_array, it, tol, rsc, csc));
     };
 
     solve(-1);
@@ -526,8 +527,8 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
         residual(n, nrhs, dA_array, ldda, dB_array, lddb, dX_array, lddx, R, stats, (it + 1) & 1,
                  batchCount, s);
     }
-    ir_final_kernel<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(n, nrhs, stats, diter_array,
-                                                                 itermax, tol, batchCount, count);
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_final_kernel<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(n, nrhs, stats, diter_array,
+                                                                 itermax, tol, batchCount, count));
     MLU_CHECK_LAUNCH();
     if (!fallback) return 0;
 
@@ -543,13 +544,13 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
     int *cidx = (int *)(w + L.cidx);
     int *cinfo = (int *)(w + L.cinfo);
     cudaMemsetAsync(count + 1, 0, sizeof(int), s);
-    ir_compact_kernel<<<batchCount, 256, 0, s>>>(n, nrhs, dA_array, dipiv_array, dB_array, lddb,
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_compact_kernel<<<batchCount, 256, 0, s>>>(n, nrhs, dA_array, dipiv_array, dB_array, lddb,
                                                  dX_array, lddx, stats, batchCount, count + 1, cA,
-                                                 cP, cX, cidx);
+                                                 cP, cX, cidx));
     rc = magma_dgesv_batched(n, nrhs, cA, ldda, cP, cX, lddx, cinfo, failed, queue);
     if (rc != 0) return rc;
-    ir_scatter_info_kernel<<<mlu_ceildiv(failed, 256), 256, 0, s>>>(failed, cidx, cinfo,
-                                                                    dinfo_array);
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_scatter_info_kernel<<<mlu_ceildiv(failed, 256), 256, 0, s>>>(failed, cidx, cinfo,
+                                                                    dinfo_array));
     MLU_CHECK_LAUNCH();
     return 0;
 }

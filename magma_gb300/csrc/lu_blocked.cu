@@ -24,13 +24,13 @@
 // No workspace and no host synchronisation: every call is stream-ordered and
 // capturable in a CUDA graph.
 #include "common.cuh"
+#include "trace.cuh"
 #include "lu_core.cuh"
 #include "solve_core.cuh"
 
 namespace mlu {
 
 constexpr int PANEL_THREADS = 256;
-constexpr int TRSM_CHUNK = 256;   // columns of U12 staged in shared memory at a time
 constexpr int SWAP_THREADS = 128;
 
 template <typename T>
@@ -44,8 +44,8 @@ panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_ar
     T *A0 = dA_array[mat];
     T *A = A0 + j0 + (size_t)j0 * ldda;
     const int info_local = panel_factor<T>(m - j0, ib, A, ldda, smem_raw, s_ipiv, j0);
-    finish_panel_step<T>(A0, ldda, n, j0, ib, ipiv_array[mat], s_ipiv,
-                         reinterpret_cast<T *>(smem_raw), TRSM_CHUNK);
+    (void)A0;
+    if (tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
     if (tid == 0) {
         if (j0 == 0) info_array[mat] = info_local;
         else if (info_local != 0 && info_array[mat] == 0) info_array[mat] = info_local;
@@ -63,10 +63,9 @@ panel_regs_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ip
     const int mat = blockIdx.x, tid = threadIdx.x;
     T *A0 = dA_array[mat];
     T *A = A0 + j0 + (size_t)j0 * ldda;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int info_local = panel_factor_regs<T, RPT>(m - j0, ib, A, ldda, s_ipiv, j0);
-    finish_panel_step<T>(A0, ldda, n, j0, ib, ipiv_array[mat], s_ipiv,
-                         reinterpret_cast<T *>(smem_raw), TRSM_CHUNK);
+    (void)A0;
+    if (tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
     if (tid == 0) {
         if (j0 == 0) info_array[mat] = info_local;
         else if (info_local != 0 && info_array[mat] == 0) info_array[mat] = info_local;
@@ -87,7 +86,7 @@ int panel_rows_per_thread(int pm)
 // Applies the interchanges of panel [j0, j0+ib) to a SWAP_COLS-column tile
 // outside the panel and, for tiles right of the panel, computes
 // U12 = L11^{-1} A12 (one thread per column).
-constexpr int SWAP_COLS = 128;
+constexpr int SWAP_COLS = 64;
 
 template <typename T>
 __global__ void __launch_bounds__(SWAP_THREADS)
@@ -95,6 +94,7 @@ swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipi
 {
     __shared__ int s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt;
     __shared__ T s_tmp[2 * PANEL_NB * (SWAP_W + 1)];
+    __shared__ T s_rhs[PANEL_NB * SWAP_COLS];
     const int mat = blockIdx.y;
     T *A = dA_array[mat];
     // column tile: left tiles cover [0, j0), right tiles cover [j0+ib, n)
@@ -113,7 +113,7 @@ swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipi
     if (threadIdx.x < 32) build_permutation(ipiv_array[mat], j0, ib, s_row, s_src, &s_cnt);
     __syncthreads();
     apply_permutation<T>(A, ldda, c0, c1, s_row, s_src, s_cnt, s_tmp);
-    if (right) trsm_l11<T>(A, ldda, j0, ib, c0, c1);
+    if (right) trsm_l11_smem<T>(A, ldda, j0, ib, c0, c1, s_rhs, SWAP_COLS);
 }
 
 // A22 -= L21 * U12 on BM x BN tiles, TM x TN accumulators per thread.
@@ -155,8 +155,7 @@ magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int 
     }
     const int pm = m - j0;
     const int rpt = panel_rows_per_thread<T>(pm);
-    const size_t trsm_smem = (size_t)PANEL_NB * TRSM_CHUNK * sizeof(T);
-    const size_t smem = rpt ? trsm_smem : max(panel_smem_bytes<T>(pm, ib), trsm_smem);
+    const size_t smem = rpt ? 0 : panel_smem_bytes<T>(pm, ib);
     if (!rpt && (smem > PANEL_SMEM_MAX || smem > panel_dyn_max))
         return MAGMA_ERR_NOT_SUPPORTED;   // m too large for a shared-memory panel
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
@@ -164,24 +163,30 @@ magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int 
         T **dAb = dA + b0;
         int **ipb = ipiv + b0;
         int *infb = info + b0;
-        // panel + interchanges + TRSM, one CTA per matrix
+        // panel (one CTA per matrix), then interchanges + TRSM (one CTA per
+        // matrix and 64-column tile)
         if (rpt == 1)
-            panel_regs_kernel<T, 1><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb);
+            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 1><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb));
         else if (rpt == 2)
-            panel_regs_kernel<T, 2><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb);
+            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 2><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb));
         else if (rpt == 4)
-            panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2)><<<nb, PANEL_THREADS, smem, s>>>(
-                m, n, j0, ib, dAb, ldda, ipb, infb);
+            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2)><<<nb, PANEL_THREADS, smem, s>>>(
+                m, n, j0, ib, dAb, ldda, ipb, infb));
         else
-            panel_kernel<T><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb);
+            MLU_LAUNCH(mlu::KC_PANEL, s, panel_kernel<T><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb));
+        const int ncl = (j0 + SWAP_COLS - 1) / SWAP_COLS;
+        const int ncr = (n - j0 - ib + SWAP_COLS - 1) / SWAP_COLS;
+        if (ncl + ncr > 0)
+            MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, swap_trsm_kernel<T><<<dim3(ncl + ncr, nb), SWAP_THREADS, 0, s>>>(m, n, j0, ib, dAb,
+                                                                          ldda, ipb));
         const int rm = m - j0 - ib, rn = n - j0 - ib;
         if (update && rm > 0 && rn > 0) {
             bool done = false;
             if (!done) {
                 const int tiles_m = (rm + BM - 1) / BM, tiles_n = (rn + BN - 1) / BN;
-                gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
+                MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
                                                  (BM / TM) * (BN / TN), 0, s>>>(
-                    m, n, j0, ib, dAb, ldda, tiles_m);
+                    m, n, j0, ib, dAb, ldda, tiles_m));
             }
         }
     }
@@ -259,9 +264,9 @@ magma_int_t blocked_getrs(bool trans, int n, int nrhs, T **dA, int ldda, int **i
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
         dim3 grid((nrhs + SOLVE_NR - 1) / SOLVE_NR, nb);
         if (trans)
-            getrs_kernel<T, true><<<grid, SOLVE_THREADS, smem, q->stream>>>(n, nrhs, dA + b0, ldda, ipiv + b0, dB + b0, lddb);
+            MLU_LAUNCH(mlu::KC_GETRS, q->stream, getrs_kernel<T, true><<<grid, SOLVE_THREADS, smem, q->stream>>>(n, nrhs, dA + b0, ldda, ipiv + b0, dB + b0, lddb));
         else
-            getrs_kernel<T, false><<<grid, SOLVE_THREADS, smem, q->stream>>>(n, nrhs, dA + b0, ldda, ipiv + b0, dB + b0, lddb);
+            MLU_LAUNCH(mlu::KC_GETRS, q->stream, getrs_kernel<T, false><<<grid, SOLVE_THREADS, smem, q->stream>>>(n, nrhs, dA + b0, ldda, ipiv + b0, dB + b0, lddb));
     }
     MLU_CHECK_LAUNCH();
     return MAGMA_SUCCESS;

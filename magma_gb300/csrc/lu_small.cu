@@ -21,6 +21,7 @@
 // search, interchanges, broadcasts) off the FP64 pipe, and the U solve reuses
 // the pivot reciprocals computed during the factorisation.
 #include "common.cuh"
+#include "trace.cuh"
 
 namespace mlu {
 
@@ -259,8 +260,8 @@ template <typename T, int N, int NRHS>
 static void launch_small_gesv(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb,
                               int *info, int batch, cudaStream_t s)
 {
-    small_gesv_kernel<T, N, NRHS><<<mlu_ceildiv(batch, GESV_WARPS), GESV_WARPS * 32, 0, s>>>(
-        n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch);
+    MLU_LAUNCH(mlu::KC_SMALL_GESV, s, small_gesv_kernel<T, N, NRHS><<<mlu_ceildiv(batch, GESV_WARPS), GESV_WARPS * 32, 0, s>>>(
+        n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch));
 }
 
 template <typename T, int N>
@@ -294,8 +295,8 @@ static void launch_small_getrs(int n, int nrhs, T **dA, int ldda, int **ipiv, T 
 {
     constexpr int NR = 4;
     dim3 grid(mlu_ceildiv(batch, SMALL_WARPS), mlu_ceildiv(nrhs, NR));
-    small_getrs_kernel<T, N, NR, TRANS><<<grid, SMALL_WARPS * 32, 0, s>>>(
-        n, nrhs, dA, ldda, ipiv, dB, lddb, batch);
+    MLU_LAUNCH(mlu::KC_GETRS, s, small_getrs_kernel<T, N, NR, TRANS><<<grid, SMALL_WARPS * 32, 0, s>>>(
+        n, nrhs, dA, ldda, ipiv, dB, lddb, batch));
 }
 
 template <typename T>

@@ -23,6 +23,7 @@
 // in a device flag (the host returns MAGMA_ERR_UNKNOWN), waits once more for
 // its own copies, frees its tensor memory and exits.
 #include "common.cuh"
+#include "trace.cuh"
 #include "lu_core.cuh"
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -344,12 +345,12 @@ static magma_int_t tc_getrf(int m, int n, float **dA, int ldda, int **ipiv, int 
             for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
                 const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
                 const int blocks = min(64, ((rm + rn) * TC_K + 255) / 256);
-                tc_stage_kernel<H><<<dim3(blocks, nb), 256, 0, q->stream>>>(
+                MLU_LAUNCH(mlu::KC_OTHER, q->stream, tc_stage_kernel<H><<<dim3(blocks, nb), 256, 0, q->stream>>>(
                     m, n, j0, ib, dA + b0, ldda, Lb + (size_t)b0 * L.pad * TC_K,
-                    Ub + (size_t)b0 * L.pad * TC_K, L.pad);
+                    Ub + (size_t)b0 * L.pad * TC_K, L.pad));
             }
-            tc_update_kernel<BF16><<<dim3(tiles_m * tiles_n, batch), 128, smem, q->stream>>>(
-                mapL, mapU, dA, ldda, m, n, j0, ib, tiles_m, err);
+            MLU_LAUNCH(mlu::KC_TC_UPDATE, q->stream, tc_update_kernel<BF16><<<dim3(tiles_m * tiles_n, batch), 128, smem, q->stream>>>(
+                mapL, mapU, dA, ldda, m, n, j0, ib, tiles_m, err));
         }
         j0 += ib;
     }

@@ -21,6 +21,7 @@
 // The _max_nocheck_work entry points never allocate or synchronise and can
 // be captured in a CUDA graph.
 #include "common.cuh"
+#include "trace.cuh"
 #include "lu_core.cuh"
 #include "solve_core.cuh"
 
@@ -75,7 +76,7 @@ vb_sort_kernel(const int *m_arr, const int *n_arr, int batch, int *order, int *c
 }
 
 template <typename T>
-__global__ void __launch_bounds__(VB_THREADS)
+__global__ void __launch_bounds__(VB_THREADS, 2)
 vb_lu_kernel(const int *m_arr, const int *n_arr, const int *nrhs_arr, T **dA_array,
              const int *ldda_arr, int **ipiv_array, T **dB_array, const int *lddb_arr,
              int *info_array, const int *order, int *counter, int batch, int smem_bytes)
@@ -101,14 +102,14 @@ vb_lu_kernel(const int *m_arr, const int *n_arr, const int *nrhs_arr, T **dA_arr
         int info = 0;
         for (int j0 = 0; j0 < mn;) {
             const int pm = m - j0;
-            // register-resident panel when it fits (pm <= 512), else shared memory
-            const int ib = pm <= 2 * VB_THREADS ? min(PANEL_NB, mn - j0)
-                                                : panel_width<T>(pm, min(PANEL_NB, mn - j0),
-                                                                 (size_t)smem_bytes);
+            // register-resident panel (one row per thread) when pm <= 256, else
+            // the shared-memory panel
+            const int ib = pm <= VB_THREADS ? min(PANEL_NB, mn - j0)
+                                            : panel_width<T>(pm, min(PANEL_NB, mn - j0),
+                                                             (size_t)smem_bytes);
             T *Ap = A + j0 + (size_t)j0 * lda;
-            const int il = pm <= VB_THREADS       ? panel_factor_regs<T, 1>(pm, ib, Ap, lda, s_ipiv, j0)
-                           : pm <= 2 * VB_THREADS ? panel_factor_regs<T, 2>(pm, ib, Ap, lda, s_ipiv, j0)
-                                                  : panel_factor<T>(pm, ib, Ap, lda, smem, s_ipiv, j0);
+            const int il = pm <= VB_THREADS ? panel_factor_regs<T, 1>(pm, ib, Ap, lda, s_ipiv, j0)
+                                            : panel_factor<T>(pm, ib, Ap, lda, smem, s_ipiv, j0);
             if (info == 0) info = il;
             if (tid < ib) ipiv[j0 + tid] = j0 + s_ipiv[tid] + 1;
             __syncthreads();
@@ -203,7 +204,7 @@ size_t vb_smem_bytes(int max_m, int max_n, int max_nrhs)
 {
     size_t need = 0;
     const int pm = max(max_m, 1);
-    if (pm > 2 * VB_THREADS)   // shorter panels live in registers
+    if (pm > VB_THREADS)   // shorter panels live in registers
         need = max(need, panel_smem_bytes<T>(pm, min(PANEL_NB, max(min(max_m, max_n), 1))));
     need = max(need, (size_t)2 * PANEL_NB * (SWAP_W + 1) * sizeof(T));
     need = max(need, (size_t)2 * PANEL_NB * 64 * sizeof(T));
@@ -223,19 +224,19 @@ magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int m
     if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(vb_lu_kernel<T>);
     const size_t smem = min(vb_smem_bytes<T>(max_m, max_n, max_nrhs), dyn_max);
     // the panel of the largest matrix must fit with at least width 1
-    if (max_m > 2 * VB_THREADS && panel_smem_bytes<T>(max_m, 1) > smem)
+    if (max_m > VB_THREADS && panel_smem_bytes<T>(max_m, 1) > smem)
         return MAGMA_ERR_NOT_SUPPORTED;
     if ((size_t)2 * PANEL_NB * 64 * sizeof(T) > smem) return MAGMA_ERR_NOT_SUPPORTED;
     if (max_nrhs > 0 && (size_t)VB_NR * max_n * sizeof(T) > smem) return MAGMA_ERR_NOT_SUPPORTED;
     int *order = (int *)work;
     int *counter = (int *)((char *)work + vb_work_bytes(batch) - 16);
-    vb_sort_kernel<<<1, 1024, 0, q->stream>>>(m, n, batch, order, counter);
+    MLU_LAUNCH(mlu::KC_OTHER, q->stream, vb_sort_kernel<<<1, 1024, 0, q->stream>>>(m, n, batch, order, counter));
     int dev = q->device, sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vb_lu_kernel<T>, VB_THREADS, smem);
     const int grid = max(1, min(batch, sms * max(per_sm, 1)));
-    vb_lu_kernel<T><<<grid, VB_THREADS, smem, q->stream>>>(m, n, nrhs, dA, ldda, ipiv, dB, lddb, info,
-                                                          order, counter, batch, (int)smem);
+    MLU_LAUNCH(mlu::KC_VB_LU, q->stream, vb_lu_kernel<T><<<grid, VB_THREADS, smem, q->stream>>>(m, n, nrhs, dA, ldda, ipiv, dB, lddb, info,
+                                                          order, counter, batch, (int)smem));
     MLU_CHECK_LAUNCH();
     return 0;
 }
@@ -257,11 +258,11 @@ magma_int_t vb_getrs_run(bool trans, const int *n, const int *nrhs, int max_n, i
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
         dim3 grid((max_nrhs + VB_NR - 1) / VB_NR, nb);
         if (trans)
-            vb_getrs_kernel<T, true><<<grid, VB_THREADS, smem, q->stream>>>(
-                n + b0, nrhs + b0, dA + b0, ldda + b0, ipiv + b0, dB + b0, lddb + b0);
+            MLU_LAUNCH(mlu::KC_GETRS, q->stream, vb_getrs_kernel<T, true><<<grid, VB_THREADS, smem, q->stream>>>(
+                n + b0, nrhs + b0, dA + b0, ldda + b0, ipiv + b0, dB + b0, lddb + b0));
         else
-            vb_getrs_kernel<T, false><<<grid, VB_THREADS, smem, q->stream>>>(
-                n + b0, nrhs + b0, dA + b0, ldda + b0, ipiv + b0, dB + b0, lddb + b0);
+            MLU_LAUNCH(mlu::KC_GETRS, q->stream, vb_getrs_kernel<T, false><<<grid, VB_THREADS, smem, q->stream>>>(
+                n + b0, nrhs + b0, dA + b0, ldda + b0, ipiv + b0, dB + b0, lddb + b0));
     }
     MLU_CHECK_LAUNCH();
     return 0;
@@ -284,7 +285,7 @@ static magma_int_t vb_check(const int *m, const int *n, const int *nrhs, const i
     }
     stats = (int *)q->work;
     cudaMemsetAsync(stats, 0, 8 * sizeof(int), q->stream);
-    vb_check_kernel<<<(batch + 255) / 256, 256, 0, q->stream>>>(m, n, nrhs, ldda, lddb, batch, stats);
+    MLU_LAUNCH(mlu::KC_OTHER, q->stream, vb_check_kernel<<<(batch + 255) / 256, 256, 0, q->stream>>>(m, n, nrhs, ldda, lddb, batch, stats));
     cudaMemcpyAsync(out, stats, 8 * sizeof(int), cudaMemcpyDeviceToHost, q->stream);
     if (cudaStreamSynchronize(q->stream) != cudaSuccess) return MAGMA_ERR_UNKNOWN;
     return 0;

@@ -7,6 +7,7 @@
 // magmablas/zset_pointer.cu:20-25 in behaviour; the queue here is a plain
 // struct around one cudaStream_t and carries no cuBLAS/cuSPARSE handles.
 #include "common.cuh"
+#include "trace.cuh"
 #include <stdlib.h>
 
 extern "C" magma_int_t magma_init(void) {
@@ -132,8 +133,8 @@ template <typename T>
 static void set_pointer(T **out, T *in, magma_int_t lda, magma_int_t row, magma_int_t column,
                         magma_int_t batch_offset, magma_int_t batch, magma_queue_t queue) {
     if (batch <= 0) return;
-    set_pointer_kernel<T><<<mlu_ceildiv(batch, 256), 256, 0, queue->stream>>>(
-        out, in, lda, row, column, (long long)batch_offset, batch);
+    MLU_LAUNCH(mlu::KC_OTHER, queue->stream, set_pointer_kernel<T><<<mlu_ceildiv(batch, 256), 256, 0, queue->stream>>>(
+        out, in, lda, row, column, (long long)batch_offset, batch));
 }
 
 extern "C" void magma_dset_pointer(double **output_array, double *input, magma_int_t lda,

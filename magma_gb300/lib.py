@@ -80,6 +80,16 @@ _PROTOS["magma_dsgesv_batched_work"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_pt
                                         c_int, c_ptr, c_ptr, c_int, C.c_double, c_int, c_ptr,
                                         C.POINTER(C.c_size_t), c_int, c_ptr], c_int)
 
+_PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
+_PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
+_PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],
+                                   c_int)
+
+# kernel classes of magma_lu_timing_start
+KERNEL_CLASSES = {"small_gesv": 1, "panel": 2, "swap_trsm": 3, "gemm": 4, "tc_update": 5,
+                  "getrs": 6, "ir_residual": 7, "ir_solve": 8, "ir_init": 9, "vb_lu": 10,
+                  "adj_ger": 11}
+
 
 def load(path: str | os.PathLike | None = None) -> C.CDLL:
     """Load libmagma_lu.so (building it first if the CUDA toolkit is present)."""
