@@ -1,7 +1,8 @@
 """Benchmark of the batched LU factor-and-solve path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dsgesv512|gesv32] [--profile]
+                    [--workload dsgesv512|gesv32|vbatched4096|adjoint2048]
+                    [--profile [--batch B]]
 
 Metric: FP64-accurate batched solves/s -- solves per second that meet the
 reference tester's accuracy bar ||b - A x||_inf / (||A||_inf ||x||_inf n eps)
@@ -920,8 +921,15 @@ def main():
     ap.add_argument("--workload", default="dsgesv512", choices=sorted(WORKLOADS))
     ap.add_argument("--profile", action="store_true",
                     help="run warm-up and timed launches only (for ncu), print nothing")
+    ap.add_argument("--batch", type=int, default=None,
+                    help="with --profile: run the workload on its first BATCH matrices "
+                         "(a small case for full ncu captures)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]()
+    if args.batch is not None:
+        if not args.profile:
+            ap.error("--batch is only for --profile runs")
+        wl.batch = args.batch
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

@@ -210,7 +210,7 @@ __device__ __forceinline__ bool ir_converged(const unsigned long long *st, int p
 // factors.  One CTA per (matrix, group of NR right-hand sides).
 template <int NR>
 __global__ void __launch_bounds__(256)
-ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, int **ipiv_array,
+ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, const int *perm,
                 double **dX_array, int lddx, const double *R, unsigned long long *stats,
                 int *iter, const int *info, int it, double tol, const double *rowscale,
                 const double *colscale)
@@ -242,13 +242,16 @@ ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, int **ipiv_array,
     const int c0 = blockIdx.x * NR;
     const int nr = min(NR, nrhs - c0);
     const double *Rm = R + ((size_t)mat * nrhs + c0) * n;
+    const int *pm = perm + (size_t)mat * n;
+    // row interchanges applied while loading: sB[i] = R[perm[i]]
     for (int e = tid; e < NR * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
-        const double rv = c < nr ? Rm[i + (size_t)c * n] : 0.0;
-        sB[c * n + i] = __double2float_rn(rowscale ? rv * rowscale[(size_t)mat * n + i] : rv);
+        const int p = pm[i];
+        const double rv = c < nr ? Rm[p + (size_t)c * n] : 0.0;
+        sB[c * n + i] = __double2float_rn(rowscale ? rv * rowscale[(size_t)mat * n + p] : rv);
     }
     __syncthreads();
-    solve_smem<float, false, NR>(n, dAs_array[mat], ldas, ipiv_array[mat], sB, nr);
+    solve_smem<float, false, NR>(n, dAs_array[mat], ldas, nullptr, sB, nr);
     double *X = dX_array[mat] + (size_t)c0 * lddx;
     for (int e = tid; e < nr * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
@@ -256,6 +259,27 @@ ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, int **ipiv_array,
         X[i + (size_t)c * lddx] = X[i + (size_t)c * lddx] +
                                   (colscale ? d * colscale[(size_t)mat * n + i] : d);
     }
+}
+
+// perm[i] = the row of the unpermuted matrix that the sequential interchanges
+// ipiv[0..n-1] bring to row i (the interchanges applied to 0..n-1), so a
+// solve can gather its right-hand side instead of swapping n times.  One CTA
+// per matrix; the interchanges are applied by one thread in shared memory.
+__global__ void ir_perm_kernel(int n, int **ipiv_array, int *perm)
+{
+    extern __shared__ int s_perm[];
+    const int mat = blockIdx.x;
+    const int *ipiv = ipiv_array[mat];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s_perm[i] = i;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < n; k++) {
+            const int p = ipiv[k] - 1;
+            if (p != k) { const int t = s_perm[k]; s_perm[k] = s_perm[p]; s_perm[p] = t; }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) perm[(size_t)mat * n + i] = s_perm[i];
 }
 
 // R = B - A X in FP64 (acc = b_i, then acc = fma(-a_ij, x_j, acc) for j = 0..n-1),
@@ -372,7 +396,7 @@ __global__ void set_float_pointers(float **out, float *base, size_t stride, int 
 static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct IrLayout {
-    size_t stats, count, asp, as, r, ca, cp, cx, cidx, cinfo, rsc, csc, tc, tc_bytes, total;
+    size_t stats, count, asp, as, r, perm, ca, cp, cx, cidx, cinfo, rsc, csc, tc, tc_bytes, total;
     int ldas;
 };
 
@@ -386,6 +410,7 @@ static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900)
     L.asp = o;   o = align256(o + (size_t)batch * sizeof(float *));
     L.as = o;    o = align256(o + (size_t)batch * n * L.ldas * sizeof(float));
     L.r = o;     o = align256(o + (size_t)batch * nrhs * n * sizeof(double));
+    L.perm = o;  o = align256(o + (size_t)batch * n * sizeof(int));
     L.ca = o;    o = align256(o + (size_t)batch * sizeof(double *));
     L.cp = o;    o = align256(o + (size_t)batch * sizeof(int *));
     L.cx = o;    o = align256(o + (size_t)batch * sizeof(double *));
@@ -505,18 +530,21 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
                                      w + L.tc, &tcb, batchCount, queue);
     }
     if (rc != 0) return rc;
+    int *perm = (int *)(w + L.perm);
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_perm_kernel<<<batchCount, 256, (size_t)n * sizeof(int), s>>>(
+        n, dipiv_array, perm));
     // right-hand sides per solve CTA: 4 when they fit, else 8
     const int snr = nrhs <= 4 ? 4 : IR_SOLVE_NR;
     const size_t ssmem = (size_t)snr * n * sizeof(float);
     auto solve = [&](int it) {
         const dim3 grid(mlu_ceildiv(nrhs, snr), batchCount);
         if (snr == 4)
-            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4><<<grid, 256, ssmem, s>>>(n, nrhs, As_array, L.ldas, dipiv_array,
-                                                        dX_array, lddx, R, stats, diter_array,
-                                                        dinfo_array, it, tol, rsc, csc));
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4><<<grid, 256, ssmem, s>>>(
+                n, nrhs, As_array, L.ldas, perm, dX_array, lddx, R, stats, diter_array,
+                dinfo_array, it, tol, rsc, csc));
         else
             MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<IR_SOLVE_NR><<<grid, 256, ssmem, s>>>(
-                n, nrhs, As_array, L.ldas, dipiv_array, dX_array, lddx, R, stats, diter_array,
+                n, nrhs, As_array, L.ldas, perm, dX_array, lddx, R, stats, diter_array,
                 dinfo_array, it, tol, rsc, csc));
     };
 

@@ -30,7 +30,7 @@
 
 namespace mlu {
 
-constexpr int PANEL_THREADS = 256;
+constexpr int PANEL_THREADS = PANEL_REGS_THREADS;
 constexpr int SWAP_THREADS = 128;
 
 template <typename T>
@@ -52,19 +52,19 @@ panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_ar
     }
 }
 
-// Register-resident panel (pm <= RPT * PANEL_THREADS): one barrier per column.
+// Register-resident panel (pm <= RPT * PANEL_THREADS): one barrier per column;
+// dynamic shared memory panel_regs_smem_bytes<T, RPT>().
 // two CTAs per SM unless the panel rows alone need more than 64 registers
 template <typename T, int RPT>
 __global__ void __launch_bounds__(PANEL_THREADS, (sizeof(T) * RPT * PANEL_NB / 4 > 64) ? 1 : 2)
 panel_regs_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
                   int *info_array)
 {
+    extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_ipiv[PANEL_NB];
     const int mat = blockIdx.x, tid = threadIdx.x;
-    T *A0 = dA_array[mat];
-    T *A = A0 + j0 + (size_t)j0 * ldda;
-    const int info_local = panel_factor_regs<T, RPT>(m - j0, ib, A, ldda, s_ipiv, j0);
-    (void)A0;
+    T *A = dA_array[mat] + j0 + (size_t)j0 * ldda;
+    const int info_local = panel_factor_regs<T, RPT>(m - j0, ib, A, ldda, s_ipiv, j0, smem);
     if (tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
     if (tid == 0) {
         if (j0 == 0) info_array[mat] = info_local;
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 gemm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int tiles_m)
 {
     __shared__ __align__(16) T sL[PANEL_NB * BM];
-    __shared__ __align__(16) T sU[PANEL_NB * BN];
+    __shared__ __align__(16) T sU[BN * GEMM_LDU];
     const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
     gemm_tile<T, BM, BN, TM, TN>(dA_array[blockIdx.y], ldda, m, n, j0, ib, j0 + ib + tm * BM,
                                  j0 + ib + tn * BN, sL, sU);
@@ -155,7 +155,10 @@ magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int 
     }
     const int pm = m - j0;
     const int rpt = panel_rows_per_thread<T>(pm);
-    const size_t smem = rpt ? 0 : panel_smem_bytes<T>(pm, ib);
+    const size_t smem = rpt == 1   ? panel_regs_smem_bytes<T, 1>()
+                        : rpt == 2 ? panel_regs_smem_bytes<T, 2>()
+                        : rpt == 4 ? panel_regs_smem_bytes<T, (sizeof(T) == 4 ? 4 : 2)>()
+                                   : panel_smem_bytes<T>(pm, ib);
     if (!rpt && (smem > PANEL_SMEM_MAX || smem > panel_dyn_max))
         return MAGMA_ERR_NOT_SUPPORTED;   // m too large for a shared-memory panel
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
@@ -223,26 +226,28 @@ template magma_int_t blocked_getrf_steps<float>(int, int, float **, int, int **,
 constexpr int SOLVE_THREADS = 256;
 constexpr int SOLVE_NR = 8;
 
-template <typename T, bool TRANS>
-__global__ void __launch_bounds__(SOLVE_THREADS, 1)
+// One CTA per (matrix, group of NR right-hand sides); NR is 4 or 8 so that a
+// call with few right-hand sides does not spend FMAs on padding columns.
+template <typename T, bool TRANS, int NR>
+__global__ void __launch_bounds__(SOLVE_THREADS)
 getrs_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T **dB_array, int lddb)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *sB = reinterpret_cast<T *>(smem_raw);   // [SOLVE_NR][n]
+    T *sB = reinterpret_cast<T *>(smem_raw);   // [NR][n]
     const int tid = threadIdx.x;
     const int mat = blockIdx.y;
-    const int c0 = blockIdx.x * SOLVE_NR;
-    const int nr = min(SOLVE_NR, nrhs - c0);
+    const int c0 = blockIdx.x * NR;
+    const int nr = min(NR, nrhs - c0);
     const T *A = dA_array[mat];
     const int *ipiv = ipiv_array[mat];
     T *B = dB_array[mat] + (size_t)c0 * lddb;
 
-    for (int e = tid; e < SOLVE_NR * n; e += blockDim.x) {
+    for (int e = tid; e < NR * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
         sB[c * n + i] = c < nr ? B[i + (size_t)c * lddb] : T(0);
     }
     __syncthreads();
-    solve_smem<T, TRANS, SOLVE_NR>(n, A, ldda, ipiv, sB, nr);
+    solve_smem<T, TRANS, NR>(n, A, ldda, ipiv, sB, nr);
     for (int e = tid; e < nr * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
         B[i + (size_t)c * lddb] = sB[c * n + i];
@@ -254,19 +259,38 @@ magma_int_t blocked_getrs(bool trans, int n, int nrhs, T **dA, int ldda, int **i
                           int lddb, int batch, magma_queue_t q)
 {
     if (batch <= 0 || n == 0 || nrhs == 0) return MAGMA_SUCCESS;
-    const size_t smem = (size_t)SOLVE_NR * n * sizeof(T);
-    static size_t dyn_max[2] = {0, 0};
-    if (!dyn_max[trans])
-        dyn_max[trans] = trans ? mlu_allow_dynamic_smem(getrs_kernel<T, true>)
-                               : mlu_allow_dynamic_smem(getrs_kernel<T, false>);
-    if (smem > dyn_max[trans]) return MAGMA_ERR_NOT_SUPPORTED;
+    const int nr = nrhs <= 4 ? 4 : SOLVE_NR;
+    const size_t smem = (size_t)nr * n * sizeof(T);
+    static size_t dyn_max[2][2] = {{0, 0}, {0, 0}};
+    size_t &dm = dyn_max[trans][nr == 4];
+    if (!dm) {
+        if (trans) dm = nr == 4 ? mlu_allow_dynamic_smem(getrs_kernel<T, true, 4>)
+                                : mlu_allow_dynamic_smem(getrs_kernel<T, true, SOLVE_NR>);
+        else dm = nr == 4 ? mlu_allow_dynamic_smem(getrs_kernel<T, false, 4>)
+                          : mlu_allow_dynamic_smem(getrs_kernel<T, false, SOLVE_NR>);
+    }
+    if (smem > dm) return MAGMA_ERR_NOT_SUPPORTED;
+    // one thread per row up to 256 (at least two warps: warp 0 solves the
+    // diagonal blocks while the others wait)
+    const int threads = min(SOLVE_THREADS, max(64, (n + 31) / 32 * 32));
+    cudaStream_t s = q->stream;
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
-        dim3 grid((nrhs + SOLVE_NR - 1) / SOLVE_NR, nb);
-        if (trans)
-            MLU_LAUNCH(mlu::KC_GETRS, q->stream, getrs_kernel<T, true><<<grid, SOLVE_THREADS, smem, q->stream>>>(n, nrhs, dA + b0, ldda, ipiv + b0, dB + b0, lddb));
+        const dim3 grid((nrhs + nr - 1) / nr, nb);
+        T **A = dA + b0, **B = dB + b0;
+        int **P = ipiv + b0;
+        if (trans && nr == 4)
+            MLU_LAUNCH(mlu::KC_GETRS, s, getrs_kernel<T, true, 4><<<grid, threads, smem, s>>>(
+                n, nrhs, A, ldda, P, B, lddb));
+        else if (trans)
+            MLU_LAUNCH(mlu::KC_GETRS, s, getrs_kernel<T, true, SOLVE_NR><<<grid, threads, smem, s>>>(
+                n, nrhs, A, ldda, P, B, lddb));
+        else if (nr == 4)
+            MLU_LAUNCH(mlu::KC_GETRS, s, getrs_kernel<T, false, 4><<<grid, threads, smem, s>>>(
+                n, nrhs, A, ldda, P, B, lddb));
         else
-            MLU_LAUNCH(mlu::KC_GETRS, q->stream, getrs_kernel<T, false><<<grid, SOLVE_THREADS, smem, q->stream>>>(n, nrhs, dA + b0, ldda, ipiv + b0, dB + b0, lddb));
+            MLU_LAUNCH(mlu::KC_GETRS, s, getrs_kernel<T, false, SOLVE_NR><<<grid, threads, smem, s>>>(
+                n, nrhs, A, ldda, P, B, lddb));
     }
     MLU_CHECK_LAUNCH();
     return MAGMA_SUCCESS;

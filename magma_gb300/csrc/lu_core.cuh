@@ -18,6 +18,7 @@ namespace mlu {
 constexpr int PANEL_NB = 32;          // largest panel width
 constexpr size_t PANEL_SMEM_MAX = 200 * 1024;   // shared memory for one panel
 constexpr int SWAP_W = 32;            // columns per gather/scatter chunk
+constexpr int GEMM_LDU = PANEL_NB + 4; // row stride of the transposed U12 tile in gemm_tile
 
 // ---------------------------------------------------------------------------
 // Panel factorisation of the pm x ib block at A (leading dimension lda) in
@@ -120,47 +121,71 @@ __device__ __forceinline__ int panel_factor(int pm, int ib, T *A, int lda, unsig
 
 // ---------------------------------------------------------------------------
 // Register-resident panel factorisation, same arithmetic as panel_factor.
-// Thread t owns rows t, t + nthr, ... (RPT of them, pm <= RPT * nthr) with
-// all ib <= 32 panel columns in registers.  One barrier per column: each warp
-// publishes its best candidate row (key, position, the row itself) into a
-// slot of a double-buffered table, then every thread reduces the table on its
-// own, so all threads agree on the pivot without a second barrier.  Row
-// positions live in registers of the owning thread.  Returns the first zero
-// pivot column + col0 (1-based) or 0, valid in thread 0; s_ipiv as in
-// panel_factor.  nthr must be a multiple of 32 and at most 1024.
+// 256 threads; thread t owns rows t + 256 r (r < RPT, pm <= 256 RPT).  The
+// column loop is a real loop (an unrolled one is tens of kilobytes of
+// straight-line code that each SM runs only a few times, and stalls on
+// instruction fetch), so registers cannot be indexed by the column.  Instead
+// a[r][0..] holds columns k..ib-1 of the row at step k: the update of step k
+// writes column j into a[r][j-1], shifting the row by one column per step
+// with no moves, and a[r][0] is always the current column.  A column leaving
+// the registers is final (an L multiplier, or an entry of the U row of a
+// pivot row, which leaves whole when it is chosen) and is stored to sP
+// (shared, ib x panel_regs_ld columns, physical row order).  One barrier per
+// column: each warp publishes its best candidate (key, position, remaining
+// row) into a double-buffered table that every warp then reduces with
+// shuffles.  Rows are written back to A in pivoted order, coalesced.
+// Returns the first zero pivot column + col0 (1-based) or 0, valid in thread
+// 0; s_ipiv[k] = position (0-based, panel-relative) chosen at step k.
+constexpr int PANEL_REGS_THREADS = 256;
+
+template <typename T, int RPT>
+__host__ __device__ constexpr int panel_regs_ld() { return PANEL_REGS_THREADS * RPT; }
+
+// shared memory that panel_factor_regs<T, RPT> needs from its caller
+template <typename T, int RPT>
+__host__ __device__ constexpr size_t panel_regs_smem_bytes()
+{
+    return (size_t)PANEL_NB * panel_regs_ld<T, RPT>() * sizeof(T) +
+           (size_t)panel_regs_ld<T, RPT>() * sizeof(int);
+}
+
 template <typename T, int RPT>
 __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, int *s_ipiv,
-                                                 int col0)
+                                                 int col0, unsigned char *smem)
 {
-    __shared__ unsigned s_hi[2][32], s_lo[2][32], s_pos[2][32];
-    __shared__ T s_row[2][32][PANEL_NB];
+    constexpr int NW = PANEL_REGS_THREADS / 32;
+    constexpr int LDP = panel_regs_ld<T, RPT>();
+    __shared__ unsigned s_hi[2][NW], s_lo[2][NW], s_pos[2][NW];
+    __shared__ __align__(16) T s_row[2][NW][PANEL_NB];
+    T *sP = reinterpret_cast<T *>(smem);
+    int *s_slot = reinterpret_cast<int *>(smem + (size_t)PANEL_NB * LDP * sizeof(T));
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nthr = blockDim.x, nwarps = nthr >> 5;
 
     T a[RPT][PANEL_NB];
     int pos[RPT];
+    bool live[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; r++) {
-        const int i = tid + r * nthr;
-        pos[r] = i < pm ? i : 0x7fffffff;          // rows past pm never become active
+        const int i = tid + r * PANEL_REGS_THREADS;
+        live[r] = i < pm;
+        pos[r] = i;
 #pragma unroll
         for (int j = 0; j < PANEL_NB; j++)
             a[r][j] = (i < pm && j < ib) ? A[i + (size_t)j * lda] : T(0);
     }
     int info_local = 0;
 
-#pragma unroll
-    for (int k = 0; k < PANEL_NB; k++) {
-        if (k >= ib) break;
+#pragma unroll 1
+    for (int k = 0; k < ib; k++) {
         const int buf = k & 1;
-        // best active row of this thread: largest key, ties to the smaller position
+        // best live row of this thread: largest key, ties to the smaller position
         unsigned long long best = 0ull;
         unsigned bpos = 0xffffffffu;
         int bslot = 0;
 #pragma unroll
         for (int r = 0; r < RPT; r++) {
-            if (pos[r] >= k && pos[r] != 0x7fffffff) {
-                const T v = a[r][k];
+            if (live[r]) {
+                const T v = a[r][0];
                 unsigned long long mag = Prec<T>::absbits(v);
                 if (Prec<T>::isnan_(v)) mag = (pos[r] == k) ? 0x7fffffffffffffffull : 0ull;
                 const unsigned long long key = mag | 0x8000000000000000ull;
@@ -169,68 +194,77 @@ __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, 
                 }
             }
         }
-        const unsigned hi = (unsigned)(best >> 32), lo = (unsigned)best;
-        const unsigned mhi = __reduce_max_sync(FULL, hi);
-        const unsigned mlo = __reduce_max_sync(FULL, hi == mhi ? lo : 0u);
-        const bool cand = hi == mhi && lo == mlo;
-        const unsigned wpos = __reduce_min_sync(FULL, cand ? bpos : 0xffffffffu);
-        const bool winner = cand && bpos == wpos && mhi != 0u;
-        if (lane == 0) { s_hi[buf][warp] = mhi; s_lo[buf][warp] = mlo; s_pos[buf][warp] = wpos; }
-        if (winner) {
+        {
+            const unsigned hi = (unsigned)(best >> 32), lo = (unsigned)best;
+            const unsigned mhi = __reduce_max_sync(FULL, hi);
+            const unsigned mlo = __reduce_max_sync(FULL, hi == mhi ? lo : 0u);
+            const bool cand = hi == mhi && lo == mlo;
+            const unsigned wpos = __reduce_min_sync(FULL, cand ? bpos : 0xffffffffu);
+            if (lane == 0) { s_hi[buf][warp] = mhi; s_lo[buf][warp] = mlo; s_pos[buf][warp] = wpos; }
+            if (cand && bpos == wpos && mhi != 0u) {
 #pragma unroll
-            for (int j = 0; j < PANEL_NB; j++) {
-                T v = a[0][j];
+                for (int j = 0; j < PANEL_NB; j++) {
+                    T v = a[0][j];
 #pragma unroll
-                for (int r = 1; r < RPT; r++) v = (bslot == r) ? a[r][j] : v;
-                s_row[buf][warp][j] = v;
-            }
-        }
-        __syncthreads();
-        // every thread reduces the warp winners
-        unsigned ghi = 0, glo = 0, gpos = 0xffffffffu;
-        int gw = 0;
-#pragma unroll
-        for (int w = 0; w < 32; w++) {
-            if (w < nwarps) {
-                const unsigned h = s_hi[buf][w], l = s_lo[buf][w], p = s_pos[buf][w];
-                if (h > ghi || (h == ghi && (l > glo || (l == glo && p < gpos)))) {
-                    ghi = h; glo = l; gpos = p; gw = w;
+                    for (int r = 1; r < RPT; r++) v = (bslot == r) ? a[r][j] : v;
+                    s_row[buf][warp][j] = v;
                 }
             }
         }
+        __syncthreads();
+        // every warp reduces the NW warp winners with shuffles
+        unsigned gpos, gw;
+        {
+            const unsigned h = lane < NW ? s_hi[buf][lane] : 0u;
+            const unsigned l = lane < NW ? s_lo[buf][lane] : 0u;
+            const unsigned p = lane < NW ? s_pos[buf][lane] : 0xffffffffu;
+            const unsigned mh = __reduce_max_sync(FULL, h);
+            const unsigned ml = __reduce_max_sync(FULL, h == mh ? l : 0u);
+            const bool c = lane < NW && h == mh && l == ml;
+            gpos = __reduce_min_sync(FULL, c ? p : 0xffffffffu);
+            gw = __ffs(__ballot_sync(FULL, c && p == gpos)) - 1;
+        }
         const T *prow = s_row[buf][gw];
-        const T piv = prow[k];
+        const T piv = prow[0];
         const bool nz = Prec<T>::nonzero(piv);
         const T rcp = T(1) / piv;
         if (tid == 0) {
             s_ipiv[k] = (int)gpos;
             if (!nz && info_local == 0) info_local = col0 + k + 1;
         }
-        // interchange of positions k and gpos, then scale and update own rows
 #pragma unroll
         for (int r = 0; r < RPT; r++) {
+            if (!live[r]) continue;
+            const int slot = tid + r * PANEL_REGS_THREADS;
+            // interchange of positions k and gpos
             if (pos[r] == (int)gpos) pos[r] = k;
             else if (pos[r] == k) pos[r] = (int)gpos;
-        }
+            if (pos[r] == k) {
+                // the pivot row: its remaining entries are U(k, k..ib-1)
 #pragma unroll
-        for (int r = 0; r < RPT; r++) {
-            if (pos[r] > k && pos[r] != 0x7fffffff) {
-                const T v = a[r][k];
-                const T l = nz ? rscale(v, piv, rcp) : v;
-                a[r][k] = l;
+                for (int j = 0; j < PANEL_NB; j++)
+                    if (j < ib - k) sP[(size_t)(k + j) * LDP + slot] = a[r][j];
+                live[r] = false;
+            } else {
+                const T l = nz ? rscale(a[r][0], piv, rcp) : a[r][0];
+                sP[(size_t)k * LDP + slot] = l;
 #pragma unroll
-                for (int j = k + 1; j < PANEL_NB; j++)
-                    if (j < ib) a[r][j] = Prec<T>::fma_(-l, prow[j], a[r][j]);
+                for (int j = 1; j < PANEL_NB; j++) a[r][j - 1] = Prec<T>::fma_(-l, prow[j], a[r][j]);
             }
         }
     }
-    // write back in pivoted order
+    // write back in pivoted order: position -> slot map, then coalesced rows
 #pragma unroll
     for (int r = 0; r < RPT; r++) {
-        if (pos[r] != 0x7fffffff) {
+        const int slot = tid + r * PANEL_REGS_THREADS;
+        if (slot < pm) s_slot[pos[r]] = slot;
+    }
+    __syncthreads();
+    for (int j = 0; j < ib; j++) {
 #pragma unroll
-            for (int j = 0; j < PANEL_NB; j++)
-                if (j < ib) A[pos[r] + (size_t)j * lda] = a[r][j];
+        for (int r = 0; r < RPT; r++) {
+            const int p = tid + r * PANEL_REGS_THREADS;
+            if (p < pm) A[p + (size_t)j * lda] = sP[(size_t)j * LDP + s_slot[p]];
         }
     }
     __syncthreads();
@@ -372,31 +406,10 @@ __device__ __forceinline__ void trsm_l11_smem(T *A, int lda, int j0, int ib, int
     __syncthreads();
 }
 
-// The rest of one panel step done by the CTA that factored the panel: write
-// the pivots, apply the panel's interchanges to every column outside the
-// panel, and solve U12 = L11^{-1} A12 for the columns right of it.  A is the
-// matrix base, ipiv its pivot vector; s_ipiv holds the panel's local pivot
-// positions.  All threads call it (it synchronises internally).
-template <typename T>
-__device__ __forceinline__ void finish_panel_step(T *A, int lda, int n, int j0, int ib, int *ipiv,
-                                                  const int *s_ipiv, T *sbuf, int chunk)
-{
-    __shared__ int s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt;
-    __shared__ T s_tmp[2 * PANEL_NB * (SWAP_W + 1)];
-    if (threadIdx.x < ib) ipiv[j0 + threadIdx.x] = j0 + s_ipiv[threadIdx.x] + 1;
-    __syncthreads();
-    if (threadIdx.x < 32) build_permutation(ipiv, j0, ib, s_row, s_src, &s_cnt);
-    __syncthreads();
-    const int cnt = s_cnt;
-    apply_permutation<T>(A, lda, 0, j0, s_row, s_src, cnt, s_tmp);
-    apply_permutation<T>(A, lda, j0 + ib, n, s_row, s_src, cnt, s_tmp);
-    if (j0 + ib < n) trsm_l11_smem<T>(A, lda, j0, ib, j0 + ib, n, sbuf, chunk);
-}
-
 // One BM x BN tile of A22 -= L21 * U12 with rows from r0 and columns from c0
 // (rows >= m or columns >= n skipped).  L21 columns j0..j0+ib, U12 rows
-// j0..j0+ib.  sL, sU: PANEL_NB x BM and PANEL_NB x BN T.  Called by exactly
-// (BM/TM)*(BN/TN) threads; synchronises on entry and exit.
+// j0..j0+ib.  sL, sU: PANEL_NB x BM and BN x GEMM_LDU T.  Called by exactly
+// (BM/TM)*(BN/TN) threads; synchronises on entry.
 template <typename T, int BM, int BN, int TM, int TN>
 __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, int ib, int r0, int c0, T *sL,
                           T *sU)
@@ -408,9 +421,11 @@ __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, i
         const int i = e % BM, k = e / BM;
         sL[k * BM + i] = (r0 + i < m) ? A[r0 + i + (size_t)(j0 + k) * lda] : T(0);
     }
+    // U12 transposed (sU[j][k], row stride GEMM_LDU): lanes run down a column
+    // of A for the load and along k for the store, both conflict-free
     for (int e = tid; e < ib * BN; e += NT) {
         const int k = e % ib, j = e / ib;
-        sU[k * BN + j] = (c0 + j < n) ? A[j0 + k + (size_t)(c0 + j) * lda] : T(0);
+        sU[j * GEMM_LDU + k] = (c0 + j < n) ? A[j0 + k + (size_t)(c0 + j) * lda] : T(0);
     }
     const int tr = tid % (BM / TM), tc = tid / (BM / TM);
     T acc[TM][TN];
@@ -424,12 +439,31 @@ __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, i
         }
     }
     __syncthreads();
-    for (int k = 0; k < ib; k++) {
+    int k = 0;
+    // four k at a time: each thread's U entries for 4 consecutive k are contiguous
+    for (; k + 4 <= ib; k += 4) {
+        T u[TN][4];
+#pragma unroll
+        for (int b = 0; b < TN; b++)
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) u[b][kk] = sU[(tc * TN + b) * GEMM_LDU + k + kk];
+#pragma unroll
+        for (int kk = 0; kk < 4; kk++) {
+            T l[TM];
+#pragma unroll
+            for (int a = 0; a < TM; a++) l[a] = sL[(k + kk) * BM + tr * TM + a];
+#pragma unroll
+            for (int a = 0; a < TM; a++)
+#pragma unroll
+                for (int b = 0; b < TN; b++) acc[a][b] = Prec<T>::fma_(-l[a], u[b][kk], acc[a][b]);
+        }
+    }
+    for (; k < ib; k++) {
         T l[TM], u[TN];
 #pragma unroll
         for (int a = 0; a < TM; a++) l[a] = sL[k * BM + tr * TM + a];
 #pragma unroll
-        for (int b = 0; b < TN; b++) u[b] = sU[k * BN + tc * TN + b];
+        for (int b = 0; b < TN; b++) u[b] = sU[(tc * TN + b) * GEMM_LDU + k];
 #pragma unroll
         for (int a = 0; a < TM; a++)
 #pragma unroll

@@ -27,7 +27,7 @@
 
 namespace mlu {
 
-constexpr int VB_THREADS = 256;
+constexpr int VB_THREADS = PANEL_REGS_THREADS;   // the register panel runs on all threads
 constexpr int VB_BINS = 1024;
 constexpr int VB_NR = 16;                  // right-hand sides per solve pass
 constexpr size_t VB_SMEM_CAP = 220 * 1024;
@@ -108,7 +108,8 @@ vb_lu_kernel(const int *m_arr, const int *n_arr, const int *nrhs_arr, T **dA_arr
                                             : panel_width<T>(pm, min(PANEL_NB, mn - j0),
                                                              (size_t)smem_bytes);
             T *Ap = A + j0 + (size_t)j0 * lda;
-            const int il = pm <= VB_THREADS ? panel_factor_regs<T, 1>(pm, ib, Ap, lda, s_ipiv, j0)
+            const int il = pm <= VB_THREADS ? panel_factor_regs<T, 1>(pm, ib, Ap, lda, s_ipiv, j0,
+                                                                      smem)
                                             : panel_factor<T>(pm, ib, Ap, lda, smem, s_ipiv, j0);
             if (info == 0) info = il;
             if (tid < ib) ipiv[j0 + tid] = j0 + s_ipiv[tid] + 1;
@@ -206,8 +207,9 @@ size_t vb_smem_bytes(int max_m, int max_n, int max_nrhs)
     const int pm = max(max_m, 1);
     if (pm > VB_THREADS)   // shorter panels live in registers
         need = max(need, panel_smem_bytes<T>(pm, min(PANEL_NB, max(min(max_m, max_n), 1))));
+    if (max_m > 0 && max_n > 0) need = max(need, panel_regs_smem_bytes<T, 1>());
     need = max(need, (size_t)2 * PANEL_NB * (SWAP_W + 1) * sizeof(T));
-    need = max(need, (size_t)2 * PANEL_NB * 64 * sizeof(T));
+    need = max(need, (size_t)(PANEL_NB + GEMM_LDU) * 64 * sizeof(T));
     if (max_nrhs > 0) need = max(need, (size_t)VB_NR * max_n * sizeof(T));
     return min(need, VB_SMEM_CAP);
 }
@@ -226,7 +228,8 @@ magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int m
     // the panel of the largest matrix must fit with at least width 1
     if (max_m > VB_THREADS && panel_smem_bytes<T>(max_m, 1) > smem)
         return MAGMA_ERR_NOT_SUPPORTED;
-    if ((size_t)2 * PANEL_NB * 64 * sizeof(T) > smem) return MAGMA_ERR_NOT_SUPPORTED;
+    if ((size_t)(PANEL_NB + GEMM_LDU) * 64 * sizeof(T) > smem) return MAGMA_ERR_NOT_SUPPORTED;
+    if (max_m > 0 && max_n > 0 && panel_regs_smem_bytes<T, 1>() > smem) return MAGMA_ERR_NOT_SUPPORTED;
     if (max_nrhs > 0 && (size_t)VB_NR * max_n * sizeof(T) > smem) return MAGMA_ERR_NOT_SUPPORTED;
     int *order = (int *)work;
     int *counter = (int *)((char *)work + vb_work_bytes(batch) - 16);

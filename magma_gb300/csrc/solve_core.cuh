@@ -68,11 +68,23 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 T acc[SOLVE_NR];
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
-                for (int t = 0; t < tb; t++) {
-                    const T l = A[i + (size_t)(t0 + t) * ldda];
+                if (tb == 32) {
+                    // the row's 32 coefficients in flight together, then the updates
+                    T lv[32];
 #pragma unroll
-                    for (int c = 0; c < SOLVE_NR; c++)
-                        acc[c] = Prec<T>::fma_(-l, sB[c * n + t0 + t], acc[c]);
+                    for (int t = 0; t < 32; t++) lv[t] = A[i + (size_t)(t0 + t) * ldda];
+#pragma unroll
+                    for (int t = 0; t < 32; t++)
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++)
+                            acc[c] = Prec<T>::fma_(-lv[t], sB[c * n + t0 + t], acc[c]);
+                } else {
+                    for (int t = 0; t < tb; t++) {
+                        const T l = A[i + (size_t)(t0 + t) * ldda];
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++)
+                            acc[c] = Prec<T>::fma_(-l, sB[c * n + t0 + t], acc[c]);
+                    }
                 }
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) sB[c * n + i] = acc[c];
@@ -88,10 +100,13 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 stage_diag_block<T>(A, ldda, t0, tb, sD);
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
+                // lane t holds U(t0+t, t0+t) and its reciprocal, computed in parallel
+                const T dl = v ? sD[lane][lane] : T(1);
+                const T rl = T(1) / dl;
                 for (int t = tb - 1; t >= 0; t--) {
                     const T u = v ? sD[lane][t] : T(0);   // U(t0+lane, t0+t)
-                    const T d = __shfl_sync(FULL, u, t);
-                    const T r = T(1) / d;
+                    const T d = __shfl_sync(FULL, dl, t);
+                    const T r = __shfl_sync(FULL, rl, t);
 #pragma unroll
                     for (int c = 0; c < SOLVE_NR; c++) {
                         const T x = rscale(__shfl_sync(FULL, y[c], t), d, r);
@@ -107,11 +122,22 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 T acc[SOLVE_NR];
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
-                for (int t = tb - 1; t >= 0; t--) {
-                    const T u = A[i + (size_t)(t0 + t) * ldda];
+                if (tb == 32) {
+                    T uv[32];
 #pragma unroll
-                    for (int c = 0; c < SOLVE_NR; c++)
-                        acc[c] = Prec<T>::fma_(-u, sB[c * n + t0 + t], acc[c]);
+                    for (int t = 0; t < 32; t++) uv[t] = A[i + (size_t)(t0 + t) * ldda];
+#pragma unroll
+                    for (int t = 31; t >= 0; t--)
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++)
+                            acc[c] = Prec<T>::fma_(-uv[t], sB[c * n + t0 + t], acc[c]);
+                } else {
+                    for (int t = tb - 1; t >= 0; t--) {
+                        const T u = A[i + (size_t)(t0 + t) * ldda];
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++)
+                            acc[c] = Prec<T>::fma_(-u, sB[c * n + t0 + t], acc[c]);
+                    }
                 }
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) sB[c * n + i] = acc[c];
@@ -128,10 +154,12 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 stage_diag_block<T>(A, ldda, t0, tb, sD);
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
+                const T dl = v ? sD[lane][lane] : T(1);
+                const T rl = T(1) / dl;
                 for (int t = 0; t < tb; t++) {
                     const T u = v ? sD[t][lane] : T(0);           // U(t0+t, t0+lane)
-                    const T d = __shfl_sync(FULL, u, t);
-                    const T r = T(1) / d;
+                    const T d = __shfl_sync(FULL, dl, t);
+                    const T r = __shfl_sync(FULL, rl, t);
 #pragma unroll
                     for (int c = 0; c < SOLVE_NR; c++) {
                         const T x = rscale(__shfl_sync(FULL, y[c], t), d, r);
@@ -148,11 +176,22 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
                 const T *Ucol = A + (size_t)i * ldda + t0;
-                for (int t = 0; t < tb; t++) {
-                    const T u = Ucol[t];
+                if (tb == 32) {
+                    T uv[32];
 #pragma unroll
-                    for (int c = 0; c < SOLVE_NR; c++)
-                        acc[c] = Prec<T>::fma_(-u, sB[c * n + t0 + t], acc[c]);
+                    for (int t = 0; t < 32; t++) uv[t] = Ucol[t];
+#pragma unroll
+                    for (int t = 0; t < 32; t++)
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++)
+                            acc[c] = Prec<T>::fma_(-uv[t], sB[c * n + t0 + t], acc[c]);
+                } else {
+                    for (int t = 0; t < tb; t++) {
+                        const T u = Ucol[t];
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++)
+                            acc[c] = Prec<T>::fma_(-u, sB[c * n + t0 + t], acc[c]);
+                    }
                 }
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) sB[c * n + i] = acc[c];
@@ -185,11 +224,22 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
                 const T *Lcol = A + (size_t)i * ldda + t0;
-                for (int t = tb - 1; t >= 0; t--) {
-                    const T l = Lcol[t];
+                if (tb == 32) {
+                    T lv[32];
 #pragma unroll
-                    for (int c = 0; c < SOLVE_NR; c++)
-                        acc[c] = Prec<T>::fma_(-l, sB[c * n + t0 + t], acc[c]);
+                    for (int t = 0; t < 32; t++) lv[t] = Lcol[t];
+#pragma unroll
+                    for (int t = 31; t >= 0; t--)
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++)
+                            acc[c] = Prec<T>::fma_(-lv[t], sB[c * n + t0 + t], acc[c]);
+                } else {
+                    for (int t = tb - 1; t >= 0; t--) {
+                        const T l = Lcol[t];
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++)
+                            acc[c] = Prec<T>::fma_(-l, sB[c * n + t0 + t], acc[c]);
+                    }
                 }
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) sB[c * n + i] = acc[c];
