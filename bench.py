@@ -162,8 +162,11 @@ class Gesv32:
         nbytes = (16 * n * n + 16 * n * r + 4 * n + 4 + 24) * self.batch
         ms = kern["launch_ms"]
         ach = flops / (ms * 1e-3) / 1e12
+        t = _traffic(self.name)
         return {"bound": "fp64", "achieved": ach, "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
-                "frac": ach / peaks["fp64_tflops"], "traffic": _traffic(self.name),
+                "frac": ach / peaks["fp64_tflops"],
+                "traffic": None if t is None else t["dram_bytes_per_unit"] * self.batch,
+                "traffic_note": None if t is None else t["note"],
                 "peak_source": "FP64 FMA-throughput probe run inside bench.py "
                                "(magma_gb300/probe/peaks.cu)",
                 **kern, "algorithmic_flops_per_launch": flops,
@@ -330,8 +333,11 @@ class Dsgesv512:
             extra = {"residual_passes_per_step": passes}
         else:
             raise ValueError(self.dominant_class)
+        t = _traffic(self.name)
+        traffic = None if t is None else t["dram_bytes_per_unit"] * passes
         return {"bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
-                "traffic": _traffic(self.name), "peak_source": src, **kern,
+                "traffic": traffic, "traffic_note": None if t is None else t["note"],
+                "peak_source": src, **kern,
                 "algorithmic_flops_per_step": flops, "algorithmic_bytes_per_step": nbytes,
                 "hbm_gbs": nbytes / (ms_step * 1e-3) / 1e9,
                 "hbm_frac_of_measured": nbytes / (ms_step * 1e-3) / 1e9 / peaks["hbm_gbs"],
@@ -621,11 +627,26 @@ WORKLOADS = {"dsgesv512": Dsgesv512, "gesv32": Gesv32, "vbatched4096": GesvVbatc
              "adjoint2048": Adjoint2048}
 
 
+# DRAM bytes (read + write) per unit of work of each workload's dominant kernel, from the ncu
+# captures summarised in profiles/ (a unit: one matrix, or one matrix-pass of the residual).
+TRAFFIC = {
+    "dsgesv512": {
+        "kernel": "mlu::ir_residual_kernel<4>", "unit": "matrix-pass (n=512, nrhs=4)",
+        "dram_bytes_per_unit": 276043776 / 128,
+        "note": "ncu capture of the first residual pass of a 128-matrix case (every matrix "
+                "active): dram__bytes_read.sum 272.84 MB + dram__bytes_write.sum 3.20 MB for 128 "
+                "matrix-passes, scaled by the residual passes of the step "
+                "(profiles/ir_residual_kernel_fp64_n512_batch128.md)"},
+    "gesv32": {
+        "kernel": "mlu::small_gesv_kernel<double,32,1>", "unit": "matrix (n=32, nrhs=1)",
+        "dram_bytes_per_unit": 110.8e6 / 10000,
+        "note": "ncu capture of one launch over 10,000 matrices: 84.9 MB read + 25.8 MB written "
+                "(profiles/small_gesv_kernel_fp64_n32_batch10000.md)"},
+}
+
+
 def _traffic(name):
-    f = ROOT / "profiles" / "traffic.json"
-    if f.exists():
-        return json.loads(f.read_text()).get(name)
-    return None
+    return TRAFFIC.get(name)
 
 
 # --------------------------------------------------------------------------
