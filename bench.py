@@ -197,13 +197,19 @@ class Dsgesv512:
     dtype = "f64 (FP32 factorisation, FP64 residual/update)"
     tol = 30.0
     itermax = 30
+    precision = "fp32"
+    FACTOR = {"fp32": "FP32 LU (SIMT FMA)",
+              "fp16": "FP32 LU with FP16 tensor-core trailing updates (FP32 accumulation, "
+                      "power-of-two row/column scaling)",
+              "bf16": "FP32 LU with BF16 tensor-core trailing updates (FP32 accumulation)"}
 
     def describe(self):
-        return {"workload": "magma_dsgesv_batched_work: 512 FP64 matrices n=512, nrhs=4, "
-                            "A=U diag(s) V^T, kappa in {1e2,1e4,1e6}; FP32 LU + FP64 refinement, "
-                            "stop at scaled residual <= 30 or 30 iterations",
+        return {"workload": "magma_dxgesv_batched_work: 512 FP64 matrices n=512, nrhs=4, "
+                            "A=U diag(s) V^T, kappa in {1e2,1e4,1e6}; " + self.FACTOR[self.precision]
+                            + " + FP64 refinement, stop at scaled residual <= 30 or 30 iterations, "
+                            "FP64 re-solve of non-converged matrices",
                 "batch": self.batch, "n": self.n, "nrhs": self.nrhs,
-                "precision": "fp32 factor, fp64 residual/update/convergence",
+                "precision": f"{self.precision} factor, fp64 residual/update/convergence",
                 "matrix": "svd-type, singular values geometric 1..1/kappa",
                 "compared_with": "magma_dgesv_batched (plain FP64) on the same inputs",
                 "l2": "inputs larger than L2: A is 1 GiB FP64"}
@@ -231,21 +237,26 @@ class Dsgesv512:
         c["ipiv"] = torch.empty((b, n), dtype=torch.int32, device=dev)
         c["info"] = torch.empty((b,), dtype=torch.int32, device=dev)
         c["iter"] = torch.empty((b,), dtype=torch.int32, device=dev)
-        c["work"] = torch.empty((mg.dsgesv_workspace_bytes(n, self.nrhs, b),), dtype=torch.uint8,
-                                device=dev)
+        c["work"] = torch.empty((mg.dsgesv_workspace_bytes(n, self.nrhs, b, self.precision),),
+                                dtype=torch.uint8, device=dev)
         c["lwork"] = C.c_size_t(c["work"].numel())
         for k in ("S", "B", "X", "ipiv"):
             c["d" + k] = ptr_array(c[k])
+        # a private copy of A per call: a matrix that falls back to the FP64 re-solve has A
+        # overwritten by its FP64 factors
+        c["Ss"] = [c["S"].clone() for _ in range(nsteps)]
+        c["dSs"] = [ptr_array(x) for x in c["Ss"]]
         return c
 
     def step(self, c, i):
+        from magma_gb300.batched import PRECISIONS
         b, n, r = self.batch, self.n, self.nrhs
-        rc = c["lib"].magma_dsgesv_batched_work(
-            n, r, vp(c["dS"]), n, vp(c["dipiv"]), vp(c["dB"]), n, vp(c["dX"]), n, vp(c["info"]),
-            vp(c["iter"]), self.itermax, self.tol, 1, vp(c["work"]), C.byref(c["lwork"]), b,
-            c["q"].handle)
+        rc = c["lib"].magma_dxgesv_batched_work(
+            PRECISIONS[self.precision], n, r, vp(c["dSs"][i]), n, vp(c["dipiv"]), vp(c["dB"]), n,
+            vp(c["dX"]), n, vp(c["info"]), vp(c["iter"]), self.itermax, self.tol, 1,
+            vp(c["work"]), C.byref(c["lwork"]), b, c["q"].handle)
         if rc != 0:
-            raise RuntimeError(f"magma_dsgesv_batched_work returned {rc}")
+            raise RuntimeError(f"magma_dxgesv_batched_work({self.precision}) returned {rc}")
 
     dominant_class = "ir_residual"
     dominant = "mlu::ir_residual_kernel<4> (FP64 residual R = B - A X)"
@@ -262,7 +273,7 @@ class Dsgesv512:
         return h2d, d2h
 
     def e2e_step(self, c):
-        c["S"].copy_(c["hS"], non_blocking=True)
+        c["Ss"][0].copy_(c["hS"], non_blocking=True)
         c["B"].copy_(c["hB"], non_blocking=True)
         self.step(c, 0)
         c["hX"].copy_(c["X"], non_blocking=True)
@@ -942,11 +953,17 @@ def main():
     ap.add_argument("--workload", default="dsgesv512", choices=sorted(WORKLOADS))
     ap.add_argument("--profile", action="store_true",
                     help="run warm-up and timed launches only (for ncu), print nothing")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "bf16"],
+                    help="dsgesv512: factorisation precision of the refinement")
     ap.add_argument("--batch", type=int, default=None,
                     help="with --profile: run the workload on its first BATCH matrices "
                          "(a small case for full ncu captures)")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]()
+    if args.precision != "fp32":
+        if args.workload != "dsgesv512":
+            ap.error("--precision applies to the dsgesv512 workload")
+        wl.precision = args.precision
     if args.batch is not None:
         if not args.profile:
             ap.error("--batch is only for --profile runs")
