@@ -387,6 +387,9 @@ class GesvVbatched:
                             "nrhs uniform in [1,16], entries uniform(-1,1); one persistent "
                             "size-sorted launch replayed from a CUDA graph",
                 "batch": self.batch, "n": "U[8,256]", "nrhs": "U[1,16]", "precision": "fp64",
+                "autotuned": {b: v for b, v in getattr(self, "tuning", {}).items()
+                              if b in ("<=16", "<=32", "<=64", "<=128", "<=256")},
+                "autotune_seconds": getattr(self, "tuning_s", None),
                 "l2": "inputs larger than L2: each step owns a private copy (~0.7 GB)"}
 
     def sizes(self):
@@ -409,8 +412,14 @@ class GesvVbatched:
     def setup(self, dev, nsteps, lib, q):
         import torch
         from magma_gb300.batched import VBatch, Queue
+        import magma_gb300 as mg
         ns, rs, As, Bs = self.host_inputs()
         c = {"ns": ns, "rs": rs, "As": As, "Bs": Bs, "lib": lib}
+        # panel width and update tile per size bin, timed on this GPU before the graphs are
+        # captured (the captured launches read the installed table)
+        t0 = time.perf_counter()
+        self.tuning = mg.autotune_vbatched(max(ns), torch.float64, q)
+        self.tuning_s = time.perf_counter() - t0
         A0 = VBatch([a.shape for a in As], ns, torch.float64, dev).load(As)
         B0 = VBatch([b.shape for b in Bs], ns, torch.float64, dev).load(Bs)
         c["A0"], c["B0"] = A0, B0

@@ -435,6 +435,55 @@ magma_int_t magma_dxgesv_batched_work(magma_int_t precision, magma_int_t n, magm
                                       void *work, size_t *lwork,
                                       magma_int_t batchCount, magma_queue_t queue);
 
+/* No counterpart in the reference: the batched refinement of
+ * magma_dxgesv_batched_work for a variable-size batch.  n[k], nrhs[k], ldda[k],
+ * lddb[k] and lddx[k] are device arrays; max_n and max_nrhs (<= 16) are their
+ * maxima, taken from the caller unchecked as in the _max_nocheck routines.
+ * precision 900 (Magma_PREC_SS): the FP32 factorisation runs in the persistent
+ * variable-size kernel.  Workspace query with work == NULL (sized by
+ * batchCount, max_n and max_nrhs).  No allocation; no synchronisation unless
+ * fallback is set.  Errors: -1 precision, -4 max_n, -5 max_nrhs, -15 itermax,
+ * -18 lwork too small, -19 lwork NULL, -20 batchCount. */
+magma_int_t magma_dxgesv_vbatched_work(magma_int_t precision, magma_int_t *n, magma_int_t *nrhs,
+                                       magma_int_t max_n, magma_int_t max_nrhs,
+                                       double **dA_array, magma_int_t *ldda,
+                                       magma_int_t **dipiv_array, double **dB_array,
+                                       magma_int_t *lddb, double **dX_array, magma_int_t *lddx,
+                                       magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                       magma_int_t itermax, double tol, magma_int_t fallback,
+                                       void *work, size_t *lwork, magma_int_t batchCount,
+                                       magma_queue_t queue);
+
+/* ------------------------------------------------------------------------
+ * Tuning of the variable-size kernel.  No counterpart in the reference, whose
+ * batched routines read fixed crossover tables
+ * (control/get_batched_crossover.cpp:300-342, 918-928).
+ *
+ * The persistent kernel of magma_?getrf_vbatched / magma_?gesv_vbatched picks,
+ * per matrix, a panel width (nb: 8, 16 or 32) and a trailing-update tile
+ * (tile: 0 = 64x64, 1 = 32x64, 2 = 32x32) from a table indexed by the size bin
+ * of max(m, n): <= 16, 32, 64, 128, 256, 512, 1024, larger (8 entries).  No
+ * choice changes a result bit: every element receives the same updates in the
+ * same order.
+ *
+ * magma_?getrf_vbatched_autotune: times every (nb in {16, 32}) x (tile)
+ * candidate on `queue`'s device for each bin up to max_n (bins above 1024 are
+ * not timed), installs the fastest in the table of that precision and returns
+ * the table in nb[8], tile[8] (either may be NULL).  Allocates its trial
+ * batches and synchronises the queue.  max_n = 0 only returns the table.
+ * Errors: -1 max_n < 0, -4 no queue, MAGMA_ERR_DEVICE_ALLOC.
+ *
+ * magma_?vbatched_tuning_get / _set: read or replace the table (8 entries
+ * each); _set returns -1 for a bad nb, -2 for a bad tile. */
+magma_int_t magma_dgetrf_vbatched_autotune(magma_int_t max_n, magma_int_t *nb, magma_int_t *tile,
+                                           magma_queue_t queue);
+magma_int_t magma_sgetrf_vbatched_autotune(magma_int_t max_n, magma_int_t *nb, magma_int_t *tile,
+                                           magma_queue_t queue);
+magma_int_t magma_dvbatched_tuning_get(magma_int_t *nb, magma_int_t *tile);
+magma_int_t magma_svbatched_tuning_get(magma_int_t *nb, magma_int_t *tile);
+magma_int_t magma_dvbatched_tuning_set(const magma_int_t *nb, const magma_int_t *tile);
+magma_int_t magma_svbatched_tuning_set(const magma_int_t *nb, const magma_int_t *tile);
+
 /* ------------------------------------------------------------------------
  * Launch accounting and kernel timing.  No counterpart in the reference,
  * whose testers time whole calls on the host

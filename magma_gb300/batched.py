@@ -271,3 +271,95 @@ def gesv_vbatched(A: "VBatch", B: "VBatch", queue: Queue | None = None):
                                                  _vp(B.ptrs), _vp(B.ld), _vp(info), b, q.handle)
     _check(rc, f"magma_{p}gesv_vbatched")
     return ipiv, offs, info
+
+
+def dxgesv_vbatched(A: "VBatch", B: "VBatch", X: "VBatch | None" = None, precision: str = "fp32",
+                    itermax: int = 30, tol: float = 0.0, fallback: bool = True,
+                    work: torch.Tensor | None = None, queue: Queue | None = None):
+    """Mixed-precision refinement of a variable-size FP64 batch
+    (magma_dxgesv_vbatched_work).  A is left intact except for matrices that fall back
+    to the FP64 re-solve; B is read; X (allocated like B when None) receives the solutions.
+    Returns (X, ipiv buffer, per-matrix ipiv offsets, info, iters)."""
+    if A.buf.dtype != torch.float64:
+        raise TypeError("dxgesv_vbatched expects float64 batches")
+    b = len(A.shapes)
+    dev = A.buf.device
+    lib = _L.load()
+    if X is None:
+        X = VBatch(B.shapes, B.nrows, torch.float64, dev)
+    max_n = max([s[0] for s in A.shapes] + [0])
+    max_r = max([s[0] for s in B.shapes] + [0])
+    tot = sum(max(s[0], 1) for s in A.shapes)
+    ipiv = torch.zeros((max(tot, 1),), dtype=torch.int32, device=dev)
+    offs, o = [], 0
+    for (nc, _) in A.shapes:
+        offs.append(o)
+        o += max(nc, 1)
+    dP = ipiv.data_ptr() + torch.tensor(offs, dtype=torch.int64, device=dev) * 4
+    info = torch.empty((b,), dtype=torch.int32, device=dev)
+    iters = torch.empty((b,), dtype=torch.int32, device=dev)
+    q = queue or Queue.current(dev)
+    lw = C.c_size_t(0)
+    args = (A.ncols, B.ncols)
+    rc = lib.magma_dxgesv_vbatched_work(PRECISIONS[precision], _vp(args[0]), _vp(args[1]), max_n,
+                                        max_r, None, None, None, None, None, None, None, None, None,
+                                        itermax, float(tol), int(fallback), None, C.byref(lw), b,
+                                        q.handle)
+    _check(rc, "magma_dxgesv_vbatched_work(query)")
+    if work is None or work.numel() < lw.value:
+        work = torch.empty((max(lw.value, 1),), dtype=torch.uint8, device=dev)
+    lw = C.c_size_t(work.numel())
+    rc = lib.magma_dxgesv_vbatched_work(PRECISIONS[precision], _vp(A.ncols), _vp(B.ncols), max_n,
+                                        max_r, _vp(A.ptrs), _vp(A.ld), _vp(dP), _vp(B.ptrs),
+                                        _vp(B.ld), _vp(X.ptrs), _vp(X.ld), _vp(info), _vp(iters),
+                                        itermax, float(tol), int(fallback), _vp(work),
+                                        C.byref(lw), b, q.handle)
+    _check(rc, "magma_dxgesv_vbatched_work")
+    return X, ipiv, offs, info, iters
+
+
+# --------------------------------------------------------------------------
+# tuning of the variable-size kernel
+
+TUNE_BINS = ("<=16", "<=32", "<=64", "<=128", "<=256", "<=512", "<=1024", ">1024")
+TILES = ("64x64", "32x64", "32x32")
+
+
+def _tune_prefix(dtype: torch.dtype) -> str:
+    if dtype == torch.float64:
+        return "d"
+    if dtype == torch.float32:
+        return "s"
+    raise TypeError(f"unsupported dtype {dtype}")
+
+
+def _tune_dict(nb, tile) -> dict:
+    return {b: {"nb": int(nb[i]), "tile": TILES[tile[i]]} for i, b in enumerate(TUNE_BINS)}
+
+
+def vbatched_tuning(dtype: torch.dtype = torch.float64) -> dict:
+    """The panel width and update tile the variable-size kernel uses per size bin."""
+    nb, tile = (C.c_int * 8)(), (C.c_int * 8)()
+    _check(getattr(_L.load(), f"magma_{_tune_prefix(dtype)}vbatched_tuning_get")(nb, tile),
+           "vbatched_tuning_get")
+    return _tune_dict(nb, tile)
+
+
+def set_vbatched_tuning(nb, tile, dtype: torch.dtype = torch.float64) -> None:
+    """Replace the table: nb and tile are 8-entry sequences (tile as index or name)."""
+    t = [TILES.index(x) if isinstance(x, str) else int(x) for x in tile]
+    nba, tia = (C.c_int * 8)(*[int(x) for x in nb]), (C.c_int * 8)(*t)
+    _check(getattr(_L.load(), f"magma_{_tune_prefix(dtype)}vbatched_tuning_set")(nba, tia),
+           "vbatched_tuning_set")
+
+
+def autotune_vbatched(max_n: int, dtype: torch.dtype = torch.float64,
+                      queue: Queue | None = None) -> dict:
+    """Time every candidate per size bin up to max_n on the current device and install the
+    fastest (magma_?getrf_vbatched_autotune).  Returns the table."""
+    q = queue or Queue.current()
+    nb, tile = (C.c_int * 8)(), (C.c_int * 8)()
+    rc = getattr(_L.load(), f"magma_{_tune_prefix(dtype)}getrf_vbatched_autotune")(
+        int(max_n), nb, tile, q.handle)
+    _check(rc, "getrf_vbatched_autotune")
+    return _tune_dict(nb, tile)

@@ -35,6 +35,12 @@ magma_int_t blocked_getrf(int m, int n, T **dA, int ldda, int **ipiv, int *info,
 template <typename T>
 magma_int_t small_gesv(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb, int *info,
                        int batch, magma_queue_t q);
+struct VbTune;
+template <typename T>
+magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int max_n, int max_nrhs,
+                   T **dA, const int *ldda, int **ipiv, T **dB, const int *lddb, int *info,
+                   void *work, int batch, magma_queue_t q, const VbTune *tune_override);
+size_t vb_work_bytes(int batch);
 }  // namespace mlu
 
 extern "C" magma_int_t magma_sgetrf_batched(magma_int_t m, magma_int_t n, float **dA_array,
@@ -65,6 +71,20 @@ constexpr int IR_ACTIVE = 0, IR_CONVERGED = 1, IR_FAILED = 2;
 //   [0] anorm bits  [1] state  [2 + par*(2*NRMAX+2) + ...] norms for parity par:
 //   rcol[NRMAX], xcol[NRMAX], rrow, xrow
 constexpr int IR_STATS_WORDS = 2 + 2 * (2 * IR_NRHS_MAX + 2);
+
+// Sizes of the batch: uniform (the scalars), or per matrix (the arrays, in
+// device memory, with the scalars holding the maxima).  Per-matrix scratch
+// (FP32 copy, residual, permutation) is laid out for the maxima: matrix k's
+// residual column c starts at R + (k * nrhs + c) * n.
+struct IrShape {
+    int n, nrhs, lda, ldb, ldx;
+    const int *n_arr, *nrhs_arr, *lda_arr, *ldb_arr, *ldx_arr;
+    __device__ __forceinline__ int N(int k) const { return n_arr ? n_arr[k] : n; }
+    __device__ __forceinline__ int NR(int k) const { return nrhs_arr ? nrhs_arr[k] : nrhs; }
+    __device__ __forceinline__ int LDA(int k) const { return lda_arr ? lda_arr[k] : lda; }
+    __device__ __forceinline__ int LDB(int k) const { return ldb_arr ? ldb_arr[k] : ldb; }
+    __device__ __forceinline__ int LDX(int k) const { return ldx_arr ? ldx_arr[k] : ldx; }
+};
 
 __device__ __forceinline__ unsigned long long dbits(double x) {
     return (unsigned long long)__double_as_longlong(x);
@@ -98,11 +118,21 @@ __device__ __forceinline__ double pow2_scale(double x)
 // 2^-e_i with max_j |a_ij| 2^-e_i in [0.5, 1) and leaves As to
 // ir_colscale_kernel.
 __global__ void __launch_bounds__(IR_ROWS)
-ir_init_kernel(int n, int nrhs, double **dA_array, int ldda, float **dAs_array, int ldas,
-               double **dB_array, int lddb, double **dX_array, int lddx, double *R,
-               unsigned long long *stats, int *iter, double *rowscale)
+ir_init_kernel(IrShape sh, double **dA_array, float **dAs_array, int ldas, double **dB_array,
+               double **dX_array, double *R, unsigned long long *stats, int *iter,
+               double *rowscale)
 {
     const int mat = blockIdx.y;
+    const int n = sh.N(mat), nrhs = sh.NR(mat);
+    const int ldda = sh.LDA(mat), lddb = sh.LDB(mat), lddx = sh.LDX(mat);
+    if (n == 0 || nrhs == 0) {                        // nothing to refine
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            stats[(size_t)mat * IR_STATS_WORDS + 1] = IR_CONVERGED;
+            iter[mat] = 0;
+        }
+        return;
+    }
+    if (blockIdx.x * IR_ROWS >= n) return;            // whole CTA past this matrix
     const int i = blockIdx.x * IR_ROWS + threadIdx.x;
     unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
     const double *A = dA_array[mat];
@@ -120,7 +150,7 @@ ir_init_kernel(int n, int nrhs, double **dA_array, int ldda, float **dAs_array, 
             mbits = ab > mbits ? ab : mbits;
             rsf += fabsf(d2f_rn_int(a));
         }
-        rowscale[(size_t)mat * n + i] = pow2_scale(__longlong_as_double((long long)mbits));
+        rowscale[(size_t)mat * sh.n + i] = pow2_scale(__longlong_as_double((long long)mbits));
         rs = (double)rsf;
     }
     if (i < n && rowscale == nullptr) {
@@ -152,9 +182,9 @@ ir_init_kernel(int n, int nrhs, double **dA_array, int ldda, float **dAs_array, 
     if (i < n) {
         const double *B = dB_array[mat];
         double *X = dX_array[mat];
-        double *Rm = R + (size_t)mat * nrhs * n;
+        double *Rm = R + (size_t)mat * sh.nrhs * sh.n;
         for (int c = 0; c < nrhs; c++) {
-            Rm[i + (size_t)c * n] = B[i + (size_t)c * lddb];
+            Rm[i + (size_t)c * sh.n] = B[i + (size_t)c * lddb];
             X[i + (size_t)c * lddx] = 0.0;
         }
     }
@@ -210,15 +240,16 @@ __device__ __forceinline__ bool ir_converged(const unsigned long long *st, int p
 // factors.  One CTA per (matrix, group of NR right-hand sides).
 template <int NR>
 __global__ void __launch_bounds__(256)
-ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, const int *perm,
-                double **dX_array, int lddx, const double *R, unsigned long long *stats,
-                int *iter, const int *info, int it, double tol, const double *rowscale,
-                const double *colscale)
+ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double **dX_array,
+                const double *R, unsigned long long *stats, int *iter, const int *info, int it,
+                double tol, const double *rowscale, const double *colscale)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *sB = reinterpret_cast<float *>(smem_raw);
     __shared__ int s_go;
     const int mat = blockIdx.y, tid = threadIdx.x;
+    const int n = sh.N(mat), nrhs = sh.NR(mat), lddx = sh.LDX(mat);
+    if ((int)blockIdx.x * NR >= nrhs || n == 0) return;   // no right-hand sides for this CTA
     unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
     if (tid == 0) {
         int go = st[1] == IR_ACTIVE;
@@ -241,14 +272,14 @@ ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, const int *perm,
     }
     const int c0 = blockIdx.x * NR;
     const int nr = min(NR, nrhs - c0);
-    const double *Rm = R + ((size_t)mat * nrhs + c0) * n;
-    const int *pm = perm + (size_t)mat * n;
+    const double *Rm = R + ((size_t)mat * sh.nrhs + c0) * sh.n;
+    const int *pm = perm + (size_t)mat * sh.n;
     // row interchanges applied while loading: sB[i] = R[perm[i]]
     for (int e = tid; e < NR * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
         const int p = pm[i];
-        const double rv = c < nr ? Rm[p + (size_t)c * n] : 0.0;
-        sB[c * n + i] = __double2float_rn(rowscale ? rv * rowscale[(size_t)mat * n + p] : rv);
+        const double rv = c < nr ? Rm[p + (size_t)c * sh.n] : 0.0;
+        sB[c * n + i] = __double2float_rn(rowscale ? rv * rowscale[(size_t)mat * sh.n + p] : rv);
     }
     __syncthreads();
     solve_smem<float, false, NR>(n, dAs_array[mat], ldas, nullptr, sB, nr);
@@ -257,7 +288,7 @@ ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, const int *perm,
         const int c = e / n, i = e % n;
         const double d = (double)sB[c * n + i];
         X[i + (size_t)c * lddx] = X[i + (size_t)c * lddx] +
-                                  (colscale ? d * colscale[(size_t)mat * n + i] : d);
+                                  (colscale ? d * colscale[(size_t)mat * sh.n + i] : d);
     }
 }
 
@@ -265,10 +296,11 @@ ir_solve_kernel(int n, int nrhs, float **dAs_array, int ldas, const int *perm,
 // ipiv[0..n-1] bring to row i (the interchanges applied to 0..n-1), so a
 // solve can gather its right-hand side instead of swapping n times.  One CTA
 // per matrix; the interchanges are applied by one thread in shared memory.
-__global__ void ir_perm_kernel(int n, int **ipiv_array, int *perm)
+__global__ void ir_perm_kernel(IrShape sh, int **ipiv_array, int *perm)
 {
     extern __shared__ int s_perm[];
     const int mat = blockIdx.x;
+    const int n = sh.N(mat);
     const int *ipiv = ipiv_array[mat];
     for (int i = threadIdx.x; i < n; i += blockDim.x) s_perm[i] = i;
     __syncthreads();
@@ -279,19 +311,22 @@ __global__ void ir_perm_kernel(int n, int **ipiv_array, int *perm)
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) perm[(size_t)mat * n + i] = s_perm[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) perm[(size_t)mat * sh.n + i] = s_perm[i];
 }
 
 // R = B - A X in FP64 (acc = b_i, then acc = fma(-a_ij, x_j, acc) for j = 0..n-1),
 // with the column and row-sum infinity norms of R and X.
 template <int NR>
 __global__ void __launch_bounds__(IR_ROWS)
-ir_residual_kernel(int n, int nrhs, double **dA_array, int ldda, double **dB_array, int lddb,
-                   double **dX_array, int lddx, double *R, unsigned long long *stats, int par)
+ir_residual_kernel(IrShape sh, double **dA_array, double **dB_array, double **dX_array, double *R,
+                   unsigned long long *stats, int par)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double *sX = reinterpret_cast<double *>(smem_raw);   // [n][NR]
     const int mat = blockIdx.y, tid = threadIdx.x;
+    const int n = sh.N(mat), nrhs = sh.NR(mat);
+    const int ldda = sh.LDA(mat), lddb = sh.LDB(mat), lddx = sh.LDX(mat);
+    if (blockIdx.x * IR_ROWS >= n) return;            // whole CTA past this matrix
     unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
     if (st[1] != IR_ACTIVE) return;
     const double *X = dX_array[mat];
@@ -313,9 +348,9 @@ ir_residual_kernel(int n, int nrhs, double **dA_array, int ldda, double **dB_arr
 #pragma unroll
             for (int c = 0; c < NR; c++) acc[c] = fma(-a, sX[j * NR + c], acc[c]);
         }
-        double *Rm = R + (size_t)mat * nrhs * n;
+        double *Rm = R + (size_t)mat * sh.nrhs * sh.n;
 #pragma unroll
-        for (int c = 0; c < NR; c++) if (c < nrhs) Rm[i + (size_t)c * n] = acc[c];
+        for (int c = 0; c < NR; c++) if (c < nrhs) Rm[i + (size_t)c * sh.n] = acc[c];
     } else {
 #pragma unroll
         for (int c = 0; c < NR; c++) acc[c] = 0.0;
@@ -337,14 +372,14 @@ ir_residual_kernel(int n, int nrhs, double **dA_array, int ldda, double **dB_arr
     atomic_max_nonneg(&nm[2 * IR_NRHS_MAX + 1], xrow);
 }
 
-__global__ void ir_final_kernel(int n, int nrhs, unsigned long long *stats, int *iter, int itermax,
+__global__ void ir_final_kernel(IrShape sh, unsigned long long *stats, int *iter, int itermax,
                                 double tol, int batch, int *failed_count)
 {
     const int mat = blockIdx.x * blockDim.x + threadIdx.x;
     if (mat >= batch) return;
     unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
     if (st[1] == IR_ACTIVE) {
-        if (ir_converged(st, itermax & 1, n, nrhs, tol)) {
+        if (ir_converged(st, itermax & 1, sh.N(mat), sh.NR(mat), tol)) {
             st[1] = IR_CONVERGED;
             iter[mat] = itermax;
         } else {
@@ -357,14 +392,15 @@ __global__ void ir_final_kernel(int n, int nrhs, unsigned long long *stats, int 
 
 // Gathers the failed matrices into compact pointer arrays and restarts their
 // X from B for the FP64 re-solve.
-__global__ void ir_compact_kernel(int n, int nrhs, double **dA_array, int **ipiv_array,
-                                  double **dB_array, int lddb, double **dX_array, int lddx,
+__global__ void ir_compact_kernel(IrShape sh, double **dA_array, int **ipiv_array,
+                                  double **dB_array, double **dX_array,
                                   const unsigned long long *stats, int batch, int *counter,
-                                  double **cA, int **cP, double **cX, int *cidx)
+                                  double **cA, int **cP, double **cX, int *cidx, int *csize)
 {
     const int mat = blockIdx.x;
     const unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
     if (st[1] != IR_FAILED) return;
+    const int n = sh.N(mat), nrhs = sh.NR(mat), lddb = sh.LDB(mat), lddx = sh.LDX(mat);
     __shared__ int slot;
     if (threadIdx.x == 0) {
         slot = atomicAdd(counter, 1);
@@ -372,6 +408,12 @@ __global__ void ir_compact_kernel(int n, int nrhs, double **dA_array, int **ipiv
         cP[slot] = ipiv_array[mat];
         cX[slot] = dX_array[mat];
         cidx[slot] = mat;
+        if (csize) {          // variable sizes: n, nrhs, ldda, lddx of the compacted batch
+            csize[slot] = n;
+            csize[batch + slot] = nrhs;
+            csize[2 * batch + slot] = sh.LDA(mat);
+            csize[3 * batch + slot] = lddx;
+        }
     }
     const double *B = dB_array[mat];
     double *X = dX_array[mat];
@@ -387,20 +429,27 @@ __global__ void ir_scatter_info_kernel(int count, const int *cidx, const int *ci
     if (k < count) info[cidx[k]] = cinfo[k];
 }
 
-__global__ void set_float_pointers(float **out, float *base, size_t stride, int batch)
+__global__ void set_float_pointers(float **out, float *base, size_t stride, int batch, int *ld_arr,
+                                   int ld)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < batch) out[k] = base + (size_t)k * stride;
+    if (k < batch) {
+        out[k] = base + (size_t)k * stride;
+        if (ld_arr) ld_arr[k] = ld;
+    }
 }
 
 static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct IrLayout {
-    size_t stats, count, asp, as, r, perm, ca, cp, cx, cidx, cinfo, rsc, csc, tc, tc_bytes, total;
+    size_t stats, count, asp, as, r, perm, ca, cp, cx, cidx, cinfo, rsc, csc, tc, tc_bytes;
+    size_t ldas_arr, csize, vbw, total;
     int ldas;
 };
 
-static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900)
+// Workspace of a refinement over `batch` matrices of order <= n with <= nrhs
+// right-hand sides; `vb` adds the arrays of a variable-size batch.
+static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900, bool vb = false)
 {
     IrLayout L;
     L.ldas = (n + 31) & ~31;
@@ -416,6 +465,12 @@ static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900)
     L.cx = o;    o = align256(o + (size_t)batch * sizeof(double *));
     L.cidx = o;  o = align256(o + (size_t)batch * sizeof(int));
     L.cinfo = o; o = align256(o + (size_t)batch * sizeof(int));
+    L.ldas_arr = L.csize = L.vbw = o;
+    if (vb) {
+        L.ldas_arr = o; o = align256(o + (size_t)batch * sizeof(int));
+        L.csize = o;    o = align256(o + 4 * (size_t)batch * sizeof(int));
+        L.vbw = o;      o = align256(o + vb_work_bytes(batch));
+    }
     L.rsc = L.csc = L.tc = o;
     L.tc_bytes = 0;
     if (prec == 905) {
@@ -436,26 +491,25 @@ static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900)
 }
 
 template <int NR>
-static void launch_residual(int n, int nrhs, double **dA, int ldda, double **dB, int lddb,
-                            double **dX, int lddx, double *R, unsigned long long *stats, int par,
-                            int batch, cudaStream_t s)
+static void launch_residual(const IrShape &sh, double **dA, double **dB, double **dX, double *R,
+                            unsigned long long *stats, int par, int batch, cudaStream_t s)
 {
-    const size_t smem = (size_t)n * NR * sizeof(double);
+    const size_t smem = (size_t)sh.n * NR * sizeof(double);
     static size_t dyn_max = 0;
     if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(ir_residual_kernel<NR>);
-    MLU_LAUNCH(mlu::KC_IR_RESIDUAL, s, ir_residual_kernel<NR><<<dim3((n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS, smem, s>>>(
-        n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par));
+    MLU_LAUNCH(mlu::KC_IR_RESIDUAL, s,
+               ir_residual_kernel<NR><<<dim3((sh.n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS, smem, s>>>(
+                   sh, dA, dB, dX, R, stats, par));
 }
 
-static void residual(int n, int nrhs, double **dA, int ldda, double **dB, int lddb, double **dX,
-                     int lddx, double *R, unsigned long long *stats, int par, int batch,
-                     cudaStream_t s)
+static void residual(const IrShape &sh, double **dA, double **dB, double **dX, double *R,
+                     unsigned long long *stats, int par, int batch, cudaStream_t s)
 {
-    if (nrhs <= 1)      launch_residual<1>(n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par, batch, s);
-    else if (nrhs <= 2) launch_residual<2>(n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par, batch, s);
-    else if (nrhs <= 4) launch_residual<4>(n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par, batch, s);
-    else if (nrhs <= 8) launch_residual<8>(n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par, batch, s);
-    else                launch_residual<16>(n, nrhs, dA, ldda, dB, lddb, dX, lddx, R, stats, par, batch, s);
+    if (sh.nrhs <= 1)      launch_residual<1>(sh, dA, dB, dX, R, stats, par, batch, s);
+    else if (sh.nrhs <= 2) launch_residual<2>(sh, dA, dB, dX, R, stats, par, batch, s);
+    else if (sh.nrhs <= 4) launch_residual<4>(sh, dA, dB, dX, R, stats, par, batch, s);
+    else if (sh.nrhs <= 8) launch_residual<8>(sh, dA, dB, dX, R, stats, par, batch, s);
+    else                   launch_residual<16>(sh, dA, dB, dX, R, stats, par, batch, s);
 }
 
 }  // namespace mlu
@@ -464,27 +518,19 @@ using namespace mlu;
 
 // The refinement driver for factorisation precision `prec`: 900 FP32
 // (Magma_PREC_SS), 905 FP16 tensor-core updates (Magma_PREC_SHT, with
-// power-of-two row and column scaling), 930 BF16 tensor-core updates.
-// Argument positions in error codes are those of magma_dsgesv_batched_work.
+// power-of-two row and column scaling), 930 BF16 tensor-core updates.  `sh`
+// holds uniform sizes, or per-matrix size arrays with their maxima (FP32
+// factorisation by the persistent variable-size kernel).  Argument checks are
+// the caller's.
 static magma_int_t
-ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrhs, double **dA_array,
-          magma_int_t ldda, magma_int_t **dipiv_array, double **dB_array, magma_int_t lddb,
-          double **dX_array, magma_int_t lddx, magma_int_t *dinfo_array, magma_int_t *diter_array,
-          magma_int_t itermax, double tol, magma_int_t fallback, void *work, size_t *lwork,
-          magma_int_t batchCount, magma_queue_t queue)
+ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array,
+       double **dB_array, double **dX_array, magma_int_t *dinfo_array, magma_int_t *diter_array,
+       magma_int_t itermax, double tol, magma_int_t fallback, void *work, size_t *lwork,
+       magma_int_t batchCount, magma_queue_t queue)
 {
-    magma_int_t info = 0;
-    if (n < 0) info = -1;
-    else if (nrhs < 0 || nrhs > IR_NRHS_MAX) info = -2;
-    else if (ldda < mlu_max(1, n)) info = -4;
-    else if (lddb < mlu_max(1, n)) info = -7;
-    else if (lddx < mlu_max(1, n)) info = -9;
-    else if (itermax < 0) info = -12;
-    if (info != 0) {
-        magma_xerbla(name, -info + argoff);
-        return info - argoff;
-    }
-    const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0), prec);
+    const bool vb = sh.n_arr != nullptr;
+    const int n = sh.n, nrhs = sh.nrhs;
+    const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0), prec, vb);
     if (work == nullptr) {          // workspace query
         *lwork = L.total;
         return 0;
@@ -507,21 +553,24 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
     float **As_array = (float **)(w + L.asp);
     float *As = (float *)(w + L.as);
     double *R = (double *)(w + L.r);
+    int *ldas_arr = vb ? (int *)(w + L.ldas_arr) : nullptr;
 
     cudaMemsetAsync(w, 0, L.asp, s);   // stats, counters
-    MLU_LAUNCH(mlu::KC_OTHER, s, set_float_pointers<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(As_array, As,
-                                                                     (size_t)n * L.ldas, batchCount));
+    MLU_LAUNCH(mlu::KC_OTHER, s, set_float_pointers<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(
+        As_array, As, (size_t)n * L.ldas, batchCount, ldas_arr, L.ldas));
     double *rsc = prec == 905 ? (double *)(w + L.rsc) : nullptr;
     double *csc = prec == 905 ? (double *)(w + L.csc) : nullptr;
     const dim3 rows_grid((n + IR_ROWS - 1) / IR_ROWS, batchCount);
-    MLU_LAUNCH(mlu::KC_IR_INIT, s, ir_init_kernel<<<rows_grid, IR_ROWS, 0, s>>>(n, nrhs, dA_array, ldda, As_array, L.ldas,
-                                                 dB_array, lddb, dX_array, lddx, R, stats,
-                                                 diter_array, rsc));
+    MLU_LAUNCH(mlu::KC_IR_INIT, s, ir_init_kernel<<<rows_grid, IR_ROWS, 0, s>>>(
+        sh, dA_array, As_array, L.ldas, dB_array, dX_array, R, stats, diter_array, rsc));
     if (rsc)
         MLU_LAUNCH(mlu::KC_IR_INIT, s, ir_colscale_kernel<<<dim3((n + 127) / 128, batchCount), 128, 0, s>>>(
-            n, dA_array, ldda, As_array, L.ldas, rsc, csc));
+            n, dA_array, sh.lda, As_array, L.ldas, rsc, csc));
     magma_int_t rc;
-    if (prec == 900) {
+    if (vb) {
+        rc = vb_run<float>(sh.n_arr, sh.n_arr, nullptr, n, n, 0, As_array, ldas_arr, dipiv_array,
+                           nullptr, nullptr, dinfo_array, w + L.vbw, batchCount, queue, nullptr);
+    } else if (prec == 900) {
         rc = magma_sgetrf_batched(n, n, As_array, L.ldas, dipiv_array, dinfo_array, batchCount,
                                   queue);
     } else {
@@ -532,7 +581,7 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
     if (rc != 0) return rc;
     int *perm = (int *)(w + L.perm);
     MLU_LAUNCH(mlu::KC_OTHER, s, ir_perm_kernel<<<batchCount, 256, (size_t)n * sizeof(int), s>>>(
-        n, dipiv_array, perm));
+        sh, dipiv_array, perm));
     // right-hand sides per solve CTA: 4 when they fit, else 8
     const int snr = nrhs <= 4 ? 4 : IR_SOLVE_NR;
     const size_t ssmem = (size_t)snr * n * sizeof(float);
@@ -540,23 +589,22 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
         const dim3 grid(mlu_ceildiv(nrhs, snr), batchCount);
         if (snr == 4)
             MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4><<<grid, 256, ssmem, s>>>(
-                n, nrhs, As_array, L.ldas, perm, dX_array, lddx, R, stats, diter_array,
-                dinfo_array, it, tol, rsc, csc));
+                sh, As_array, L.ldas, perm, dX_array, R, stats, diter_array, dinfo_array, it,
+                tol, rsc, csc));
         else
             MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<IR_SOLVE_NR><<<grid, 256, ssmem, s>>>(
-                n, nrhs, As_array, L.ldas, perm, dX_array, lddx, R, stats, diter_array,
-                dinfo_array, it, tol, rsc, csc));
+                sh, As_array, L.ldas, perm, dX_array, R, stats, diter_array, dinfo_array, it,
+                tol, rsc, csc));
     };
 
     solve(-1);
-    residual(n, nrhs, dA_array, ldda, dB_array, lddb, dX_array, lddx, R, stats, 0, batchCount, s);
+    residual(sh, dA_array, dB_array, dX_array, R, stats, 0, batchCount, s);
     for (int it = 0; it < itermax; it++) {
         solve(it);
-        residual(n, nrhs, dA_array, ldda, dB_array, lddb, dX_array, lddx, R, stats, (it + 1) & 1,
-                 batchCount, s);
+        residual(sh, dA_array, dB_array, dX_array, R, stats, (it + 1) & 1, batchCount, s);
     }
-    MLU_LAUNCH(mlu::KC_OTHER, s, ir_final_kernel<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(n, nrhs, stats, diter_array,
-                                                                 itermax, tol, batchCount, count));
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_final_kernel<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(
+        sh, stats, diter_array, itermax, tol, batchCount, count));
     MLU_CHECK_LAUNCH();
     if (!fallback) return 0;
 
@@ -571,16 +619,47 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
     double **cX = (double **)(w + L.cx);
     int *cidx = (int *)(w + L.cidx);
     int *cinfo = (int *)(w + L.cinfo);
+    int *csize = vb ? (int *)(w + L.csize) : nullptr;
     cudaMemsetAsync(count + 1, 0, sizeof(int), s);
-    MLU_LAUNCH(mlu::KC_OTHER, s, ir_compact_kernel<<<batchCount, 256, 0, s>>>(n, nrhs, dA_array, dipiv_array, dB_array, lddb,
-                                                 dX_array, lddx, stats, batchCount, count + 1, cA,
-                                                 cP, cX, cidx));
-    rc = magma_dgesv_batched(n, nrhs, cA, ldda, cP, cX, lddx, cinfo, failed, queue);
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_compact_kernel<<<batchCount, 256, 0, s>>>(
+        sh, dA_array, dipiv_array, dB_array, dX_array, stats, batchCount, count + 1, cA, cP, cX,
+        cidx, csize));
+    if (vb)
+        rc = vb_run<double>(csize, csize, csize + batchCount, n, n, nrhs, cA, csize + 2 * batchCount,
+                            cP, cX, csize + 3 * batchCount, cinfo, w + L.vbw, failed, queue,
+                            nullptr);
+    else
+        rc = magma_dgesv_batched(n, nrhs, cA, sh.lda, cP, cX, sh.ldx, cinfo, failed, queue);
     if (rc != 0) return rc;
-    MLU_LAUNCH(mlu::KC_OTHER, s, ir_scatter_info_kernel<<<mlu_ceildiv(failed, 256), 256, 0, s>>>(failed, cidx, cinfo,
-                                                                    dinfo_array));
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_scatter_info_kernel<<<mlu_ceildiv(failed, 256), 256, 0, s>>>(
+        failed, cidx, cinfo, dinfo_array));
     MLU_CHECK_LAUNCH();
     return 0;
+}
+
+// Argument checks of magma_dsgesv_batched_work (positions shifted by argoff),
+// then the uniform refinement.
+static magma_int_t
+ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrhs, double **dA_array,
+          magma_int_t ldda, magma_int_t **dipiv_array, double **dB_array, magma_int_t lddb,
+          double **dX_array, magma_int_t lddx, magma_int_t *dinfo_array, magma_int_t *diter_array,
+          magma_int_t itermax, double tol, magma_int_t fallback, void *work, size_t *lwork,
+          magma_int_t batchCount, magma_queue_t queue)
+{
+    magma_int_t info = 0;
+    if (n < 0) info = -1;
+    else if (nrhs < 0 || nrhs > IR_NRHS_MAX) info = -2;
+    else if (ldda < mlu_max(1, n)) info = -4;
+    else if (lddb < mlu_max(1, n)) info = -7;
+    else if (lddx < mlu_max(1, n)) info = -9;
+    else if (itermax < 0) info = -12;
+    if (info != 0) {
+        magma_xerbla(name, -info + argoff);
+        return info - argoff;
+    }
+    const IrShape sh = {n, nrhs, ldda, lddb, lddx, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return ir_run(prec, sh, dA_array, dipiv_array, dB_array, dX_array, dinfo_array, diter_array,
+                  itermax, tol, fallback, work, lwork, batchCount, queue);
 }
 
 extern "C" magma_int_t
@@ -639,4 +718,38 @@ magma_dsgesv_batched(magma_int_t n, magma_int_t nrhs, double **dA_array, magma_i
     return magma_dsgesv_batched_work(n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb,
                                      dX_array, lddx, dinfo_array, diter_array, 30, 0.0, 1,
                                      queue->work, &lwork, batchCount, queue);
+}
+
+// ---------------------------------------------------------------------------
+// Variable-size refinement (no counterpart in the reference).
+
+extern "C" magma_int_t
+magma_dxgesv_vbatched_work(magma_int_t precision, magma_int_t *n, magma_int_t *nrhs,
+                           magma_int_t max_n, magma_int_t max_nrhs, double **dA_array,
+                           magma_int_t *ldda, magma_int_t **dipiv_array, double **dB_array,
+                           magma_int_t *lddb, double **dX_array, magma_int_t *lddx,
+                           magma_int_t *dinfo_array, magma_int_t *diter_array,
+                           magma_int_t itermax, double tol, magma_int_t fallback, void *work,
+                           size_t *lwork, magma_int_t batchCount, magma_queue_t queue)
+{
+    magma_int_t info = 0;
+    if (precision != 900) info = -1;
+    else if (max_n < 0) info = -4;
+    else if (max_nrhs < 0 || max_nrhs > IR_NRHS_MAX) info = -5;
+    else if (itermax < 0) info = -15;
+    else if (lwork == nullptr) info = -19;
+    else if (batchCount < 0) info = -20;
+    if (info != 0) {
+        magma_xerbla(__func__, -info);
+        return info;
+    }
+    const IrShape sh = {max_n, max_nrhs, 0, 0, 0, n, nrhs, ldda, lddb, lddx};
+    if (work != nullptr) {
+        size_t need = 0;
+        ir_run(900, sh, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, itermax, tol, 0,
+               nullptr, &need, batchCount, queue);
+        if (*lwork < need) return -18;
+    }
+    return ir_run(900, sh, dA_array, dipiv_array, dB_array, dX_array, dinfo_array, diter_array,
+                  itermax, tol, fallback, work, lwork, batchCount, queue);
 }

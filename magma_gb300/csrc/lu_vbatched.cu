@@ -25,12 +25,43 @@
 #include "lu_core.cuh"
 #include "solve_core.cuh"
 
+#include <mutex>
+#include <vector>
+
 namespace mlu {
 
 constexpr int VB_THREADS = PANEL_REGS_THREADS;   // the register panel runs on all threads
 constexpr int VB_BINS = 1024;
 constexpr int VB_NR = 16;                  // right-hand sides per solve pass
 constexpr size_t VB_SMEM_CAP = 220 * 1024;
+
+// Per-size-bin tuning of the persistent kernel: panel width and trailing-update
+// tile shape for matrices whose max(m, n) falls in bin b (<= 16, 32, 64, 128,
+// 256, 512, 1024, larger).  Every choice applies the same updates to every
+// element in the same order, so the tuning never changes a result.
+constexpr int VB_TUNE_BINS = 8;
+enum VbTile { VB_TILE_64x64 = 0, VB_TILE_32x64 = 1, VB_TILE_32x32 = 2, VB_TILE_COUNT = 3 };
+struct VbTune {
+    unsigned char nb[VB_TUNE_BINS];     // panel width: 8, 16 or 32
+    unsigned char tile[VB_TUNE_BINS];   // VbTile
+};
+
+__host__ __device__ inline int vb_tune_bin(int mx)
+{
+    int b = 0;
+    for (int ub = 16; b < VB_TUNE_BINS - 1 && mx > ub; ub <<= 1) b++;
+    return b;
+}
+
+// all tiles of the trailing update of one step, BM x BN tiles
+template <typename T, int BM, int BN, int TM, int TN>
+__device__ __forceinline__ void vb_update(T *A, int lda, int m, int n, int j0, int ib, T *sL, T *sU)
+{
+    const int rm = m - j0 - ib, rn = n - j0 - ib;
+    for (int tn = 0; tn < rn; tn += BN)
+        for (int tm = 0; tm < rm; tm += BM)
+            gemm_tile<T, BM, BN, TM, TN>(A, lda, m, n, j0, ib, j0 + ib + tm, j0 + ib + tn, sL, sU);
+}
 
 __device__ __forceinline__ int vb_key(int m, int n) { return min(max(max(m, n), 0), VB_BINS - 1); }
 
@@ -79,7 +110,8 @@ template <typename T>
 __global__ void __launch_bounds__(VB_THREADS, 2)
 vb_lu_kernel(const int *m_arr, const int *n_arr, const int *nrhs_arr, T **dA_array,
              const int *ldda_arr, int **ipiv_array, T **dB_array, const int *lddb_arr,
-             int *info_array, const int *order, int *counter, int batch, int smem_bytes)
+             int *info_array, const int *order, int *counter, int batch, int smem_bytes,
+             VbTune tune)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_item, s_ipiv[PANEL_NB], s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt;
@@ -99,13 +131,15 @@ vb_lu_kernel(const int *m_arr, const int *n_arr, const int *nrhs_arr, T **dA_arr
         T *B = nrhs > 0 ? dB_array[k] : nullptr;
         const int ldb = nrhs > 0 ? lddb_arr[k] : 1;
         const int mn = min(m, n);
+        const int bin = vb_tune_bin(max(m, n));
+        const int nbw = tune.nb[bin], tile = tune.tile[bin];
         int info = 0;
         for (int j0 = 0; j0 < mn;) {
             const int pm = m - j0;
             // register-resident panel (one row per thread) when pm <= 256, else
             // the shared-memory panel
-            const int ib = pm <= VB_THREADS ? min(PANEL_NB, mn - j0)
-                                            : panel_width<T>(pm, min(PANEL_NB, mn - j0),
+            const int ib = pm <= VB_THREADS ? min(nbw, mn - j0)
+                                            : panel_width<T>(pm, min(nbw, mn - j0),
                                                              (size_t)smem_bytes);
             T *Ap = A + j0 + (size_t)j0 * lda;
             const int il = pm <= VB_THREADS ? panel_factor_regs<T, 1>(pm, ib, Ap, lda, s_ipiv, j0,
@@ -124,12 +158,13 @@ vb_lu_kernel(const int *m_arr, const int *n_arr, const int *nrhs_arr, T **dA_arr
             }
             if (j0 + ib < n) {
                 trsm_l11_smem<T>(A, lda, j0, ib, j0 + ib, n, sT, 64);
-                const int rm = m - j0 - ib, rn = n - j0 - ib;
                 T *sL = sT, *sU = sT + PANEL_NB * 64;
-                for (int tn = 0; tn < rn; tn += 64)
-                    for (int tm = 0; tm < rm; tm += 64)
-                        gemm_tile<T, 64, 64, 4, 4>(A, lda, m, n, j0, ib, j0 + ib + tm, j0 + ib + tn,
-                                                   sL, sU);
+                if (tile == VB_TILE_32x32)
+                    vb_update<T, 32, 32, 2, 2>(A, lda, m, n, j0, ib, sL, sU);
+                else if (tile == VB_TILE_32x64)
+                    vb_update<T, 32, 64, 2, 4>(A, lda, m, n, j0, ib, sL, sU);
+                else
+                    vb_update<T, 64, 64, 4, 4>(A, lda, m, n, j0, ib, sL, sU);
                 __syncthreads();
             }
             j0 += ib;
@@ -214,13 +249,28 @@ size_t vb_smem_bytes(int max_m, int max_n, int max_nrhs)
     return min(need, VB_SMEM_CAP);
 }
 
-inline size_t vb_work_bytes(int batch) { return ((size_t)batch * sizeof(int) + 16 + 255) & ~(size_t)255; }
+size_t vb_work_bytes(int batch) { return ((size_t)batch * sizeof(int) + 16 + 255) & ~(size_t)255; }
+
+// Tuning tables in use (one per precision), set by magma_?vbatched_tuning_set
+// or the autotuner.  Defaults: the autotuner's choices on GB300.
+static std::mutex g_tune_mu;
+static VbTune g_tune[2] = {
+    {{32, 32, 32, 32, 32, 32, 32, 32}, {0, 0, 0, 0, 0, 0, 0, 0}},   // double
+    {{32, 32, 32, 32, 32, 32, 32, 32}, {0, 0, 0, 0, 0, 0, 0, 0}},   // float
+};
+template <typename T> inline int tune_index() { return sizeof(T) == 8 ? 0 : 1; }
+template <typename T> static VbTune current_tune()
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return g_tune[tune_index<T>()];
+}
 
 template <typename T>
 magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int max_n, int max_nrhs,
                    T **dA, const int *ldda, int **ipiv, T **dB, const int *lddb, int *info,
-                   void *work, int batch, magma_queue_t q)
+                   void *work, int batch, magma_queue_t q, const VbTune *tune_override = nullptr)
 {
+    const VbTune tune = tune_override ? *tune_override : current_tune<T>();
     if (batch <= 0) return 0;
     static size_t dyn_max = 0;
     if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(vb_lu_kernel<T>);
@@ -239,10 +289,17 @@ magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int m
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vb_lu_kernel<T>, VB_THREADS, smem);
     const int grid = max(1, min(batch, sms * max(per_sm, 1)));
     MLU_LAUNCH(mlu::KC_VB_LU, q->stream, vb_lu_kernel<T><<<grid, VB_THREADS, smem, q->stream>>>(m, n, nrhs, dA, ldda, ipiv, dB, lddb, info,
-                                                          order, counter, batch, (int)smem));
+                                                          order, counter, batch, (int)smem, tune));
     MLU_CHECK_LAUNCH();
     return 0;
 }
+
+template magma_int_t vb_run<double>(const int *, const int *, const int *, int, int, int, double **,
+                                    const int *, int **, double **, const int *, int *, void *,
+                                    int, magma_queue_t, const VbTune *);
+template magma_int_t vb_run<float>(const int *, const int *, const int *, int, int, int, float **,
+                                   const int *, int **, float **, const int *, int *, void *, int,
+                                   magma_queue_t, const VbTune *);
 
 template <typename T>
 magma_int_t vb_getrs_run(bool trans, const int *n, const int *nrhs, int max_n, int max_nrhs, T **dA,
@@ -476,4 +533,209 @@ extern "C" magma_int_t magma_sgetrs_vbatched(magma_trans_t trans, magma_int_t *n
 {
     return getrs_vbatched<float>(__func__, trans, n, nrhs, dA_array, ldda, dipiv_array, dB_array,
                                  lddb, batchCount, queue);
+}
+
+// ---------------------------------------------------------------------------
+// Tuning of the persistent kernel (no counterpart in the reference, whose
+// batched tuning is a set of fixed crossover tables,
+// control/get_batched_crossover.cpp:300-342, 918-928).
+
+namespace mlu {
+
+// uniform(-1, 1) entries from a counter-based hash (splitmix64) for the
+// autotuner's trial batches
+template <typename T>
+__global__ void vb_fill_kernel(T *buf, size_t count, unsigned long long seed)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count;
+         i += (size_t)gridDim.x * blockDim.x) {
+        unsigned long long x = seed + i * 0x9e3779b97f4a7c15ull;
+        x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+        x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+        x ^= x >> 31;
+        buf[i] = (T)((double)(x >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+    }
+}
+
+// pointer and size arrays of a uniform trial batch of k matrices of order n
+template <typename T>
+__global__ void vb_trial_arrays_kernel(int k, int n, T *A, int *P, T **dA, int **dP, int *dn,
+                                       int *dld)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    dA[i] = A + (size_t)i * n * n;
+    dP[i] = P + (size_t)i * n;
+    dn[i] = n;
+    dld[i] = n;
+}
+
+static const int VB_TUNE_NB[] = {16, 32};
+constexpr int VB_TUNE_MAX_N = 1024;   // bins above this keep their table entry
+
+template <typename T>
+static magma_int_t vb_autotune(int max_n, magma_queue_t q, VbTune *out)
+{
+    VbTune t = current_tune<T>();
+    cudaStream_t s = q->stream;
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, q->device);
+    magma_int_t rc = MAGMA_SUCCESS;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cudaGetLastError();
+        return MAGMA_ERR_UNKNOWN;
+    }
+    int ub = 16;
+    for (int b = 0; b < VB_TUNE_BINS && rc == MAGMA_SUCCESS; b++, ub <<= 1) {
+        const int lo = b == 0 ? 1 : ub / 2 + 1;
+        if (lo > max_n || lo > VB_TUNE_MAX_N) break;
+        // representative order: three quarters of the bin's upper bound
+        const int n = max(lo, min(min(max_n, VB_TUNE_MAX_N), 3 * ub / 4));
+        const size_t smem = vb_smem_bytes<T>(n, n, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vb_lu_kernel<T>, VB_THREADS, smem);
+        const double flops = 2.0 / 3.0 * n * (double)n * n;
+        const int resident = sms * max(per_sm, 1);
+        // enough matrices to keep every resident CTA busy several times over,
+        // about 2 GFLOP per trial, at most 4096
+        const int k = max(2 * resident, min(4096, (int)(2e9 / flops)));
+        T *A = nullptr, **dA = nullptr;
+        int *P = nullptr, **dP = nullptr, *dn = nullptr, *dld = nullptr, *info = nullptr;
+        void *work = nullptr;
+        const size_t wb = vb_work_bytes(k);
+        if (cudaMalloc(&A, (size_t)k * n * n * sizeof(T)) != cudaSuccess ||
+            cudaMalloc(&P, (size_t)k * n * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&dA, k * sizeof(T *)) != cudaSuccess ||
+            cudaMalloc(&dP, k * sizeof(int *)) != cudaSuccess ||
+            cudaMalloc(&dn, k * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&dld, k * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&info, k * sizeof(int)) != cudaSuccess ||
+            cudaMalloc(&work, wb) != cudaSuccess) {
+            cudaGetLastError();
+            rc = MAGMA_ERR_DEVICE_ALLOC;
+        }
+        if (rc == MAGMA_SUCCESS) {
+            MLU_LAUNCH(mlu::KC_OTHER, s, vb_trial_arrays_kernel<T><<<(k + 255) / 256, 256, 0, s>>>(
+                k, n, A, P, dA, dP, dn, dld));
+            float best = -1.f;
+            int best_nb = t.nb[b], best_tile = t.tile[b];
+            for (int nbw : VB_TUNE_NB) {
+                for (int tile = 0; tile < VB_TILE_COUNT && rc == MAGMA_SUCCESS; tile++) {
+                    VbTune trial = t;
+                    trial.nb[b] = (unsigned char)nbw;
+                    trial.tile[b] = (unsigned char)tile;
+                    float tmin = -1.f;
+                    for (int rep = 0; rep < 2; rep++) {
+                        MLU_LAUNCH(mlu::KC_OTHER, s, vb_fill_kernel<T><<<4 * sms, 256, 0, s>>>(
+                            A, (size_t)k * n * n, 0x5eedull + 977ull * b));
+                        cudaEventRecord(e0, s);
+                        rc = vb_run<T>(dn, dn, nullptr, n, n, 0, dA, dld, dP, nullptr, nullptr,
+                                       info, work, k, q, &trial);
+                        cudaEventRecord(e1, s);
+                        float ms = 0.f;
+                        if (rc != MAGMA_SUCCESS || cudaEventSynchronize(e1) != cudaSuccess ||
+                            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                            cudaGetLastError();
+                            if (rc == MAGMA_SUCCESS) rc = MAGMA_ERR_UNKNOWN;
+                            break;
+                        }
+                        if (tmin < 0.f || ms < tmin) tmin = ms;
+                    }
+                    if (rc == MAGMA_SUCCESS && (best < 0.f || tmin < best)) {
+                        best = tmin;
+                        best_nb = nbw;
+                        best_tile = tile;
+                    }
+                }
+            }
+            t.nb[b] = (unsigned char)best_nb;
+            t.tile[b] = (unsigned char)best_tile;
+        }
+        cudaFree(A); cudaFree(P); cudaFree(dA); cudaFree(dP); cudaFree(dn); cudaFree(dld);
+        cudaFree(info); cudaFree(work);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != MAGMA_SUCCESS) return rc;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[tune_index<T>()] = t;
+    }
+    if (out) *out = t;
+    return MAGMA_SUCCESS;
+}
+
+template <typename T>
+static magma_int_t tuning_get(magma_int_t *nb, magma_int_t *tile)
+{
+    const VbTune t = current_tune<T>();
+    for (int b = 0; b < VB_TUNE_BINS; b++) {
+        if (nb) nb[b] = t.nb[b];
+        if (tile) tile[b] = t.tile[b];
+    }
+    return MAGMA_SUCCESS;
+}
+
+template <typename T>
+static magma_int_t tuning_set(const magma_int_t *nb, const magma_int_t *tile)
+{
+    if (nb == nullptr) return -1;
+    if (tile == nullptr) return -2;
+    VbTune t;
+    for (int b = 0; b < VB_TUNE_BINS; b++) {
+        if (nb[b] != 8 && nb[b] != 16 && nb[b] != 32) return -1;
+        if (tile[b] < 0 || tile[b] >= VB_TILE_COUNT) return -2;
+        t.nb[b] = (unsigned char)nb[b];
+        t.tile[b] = (unsigned char)tile[b];
+    }
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[tune_index<T>()] = t;
+    return MAGMA_SUCCESS;
+}
+
+template <typename T>
+static magma_int_t autotune_entry(magma_int_t max_n, magma_int_t *nb, magma_int_t *tile,
+                                  magma_queue_t queue)
+{
+    if (max_n < 0) return -1;
+    if (queue == nullptr) return -4;
+    if (max_n == 0) return tuning_get<T>(nb, tile);
+    VbTune t;
+    const magma_int_t rc = vb_autotune<T>(max_n, queue, &t);
+    if (rc != MAGMA_SUCCESS) return rc;
+    return tuning_get<T>(nb, tile);
+}
+
+}  // namespace mlu
+
+extern "C" magma_int_t magma_dgetrf_vbatched_autotune(magma_int_t max_n, magma_int_t *nb,
+                                                      magma_int_t *tile, magma_queue_t queue)
+{
+    return mlu::autotune_entry<double>(max_n, nb, tile, queue);
+}
+
+extern "C" magma_int_t magma_sgetrf_vbatched_autotune(magma_int_t max_n, magma_int_t *nb,
+                                                      magma_int_t *tile, magma_queue_t queue)
+{
+    return mlu::autotune_entry<float>(max_n, nb, tile, queue);
+}
+
+extern "C" magma_int_t magma_dvbatched_tuning_get(magma_int_t *nb, magma_int_t *tile)
+{
+    return mlu::tuning_get<double>(nb, tile);
+}
+
+extern "C" magma_int_t magma_svbatched_tuning_get(magma_int_t *nb, magma_int_t *tile)
+{
+    return mlu::tuning_get<float>(nb, tile);
+}
+
+extern "C" magma_int_t magma_dvbatched_tuning_set(const magma_int_t *nb, const magma_int_t *tile)
+{
+    return mlu::tuning_set<double>(nb, tile);
+}
+
+extern "C" magma_int_t magma_svbatched_tuning_set(const magma_int_t *nb, const magma_int_t *tile)
+{
+    return mlu::tuning_set<float>(nb, tile);
 }

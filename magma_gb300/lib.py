@@ -80,6 +80,14 @@ _PROTOS["magma_dsgesv_batched_work"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_pt
                                         c_int, c_ptr, c_ptr, c_int, C.c_double, c_int, c_ptr,
                                         C.POINTER(C.c_size_t), c_int, c_ptr], c_int)
 
+for _p in "ds":
+    _PROTOS[f"magma_{_p}getrf_vbatched_autotune"] = ([c_int, c_ptr, c_ptr, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}vbatched_tuning_get"] = ([c_ptr, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}vbatched_tuning_set"] = ([c_ptr, c_ptr], c_int)
+_PROTOS["magma_dxgesv_vbatched_work"] = ([c_int, c_ptr, c_ptr, c_int, c_int, c_ptr, c_ptr, c_ptr,
+                                          c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_int,
+                                          C.c_double, c_int, c_ptr, C.POINTER(C.c_size_t), c_int,
+                                          c_ptr], c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
 _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],

@@ -181,6 +181,18 @@ def dgesv_vbatched(ns, nrhss, As, Bs, nthreads=None):
     return pivs, info
 
 
+def sgesv_vbatched(ns, nrhss, As, Bs):
+    """FP32 variable-size batch, same conventions as dgesv_vbatched (oracle_sgetrf + oracle_sgetrs
+    per matrix, the solve applied whatever info is)."""
+    pivs, info = [], np.zeros(len(ns), dtype=np.int32)
+    for k in range(len(ns)):
+        p, info[k] = sgetrf(As[k], ns[k])
+        if nrhss[k] > 0 and ns[k] > 0:
+            sgetrs(As[k], p, Bs[k])
+        pivs.append(p[:ns[k]].copy())
+    return pivs, info
+
+
 def dsgesv_batched(A, B, itermax=30, tol=0.0, fallback=True, nthreads=None):
     """Mixed-precision IR restatement (oracle_dsgesv).  A: (batch, n, ld) FP64
     storage, modified only for matrices that fall back; B: (batch, nrhs, ldb).
@@ -201,6 +213,20 @@ def dsgesv_batched(A, B, itermax=30, tol=0.0, fallback=True, nthreads=None):
        ipiv.shape[1], _p(info), _p(iters), itermax, float(tol), 1 if fallback else 0, b,
        _threads(nthreads))
     return X, ipiv, info, iters
+
+
+def dsgesv_vbatched(As, Bs, itermax=30, tol=0.0, fallback=True):
+    """Variable-size refinement: oracle_dsgesv per matrix.  As[k]: (n_k, ld_k) storage,
+    Bs[k]: (nrhs_k, ldb_k).  Returns (Xs, ipivs, info, iters)."""
+    Xs, pivs = [], []
+    info = np.zeros(len(As), dtype=np.int32)
+    iters = np.zeros(len(As), dtype=np.int32)
+    for k, (A, B) in enumerate(zip(As, Bs)):
+        X, p, inf, it = dsgesv_batched(A[None], B[None], itermax, tol, fallback, nthreads=1)
+        Xs.append(X[0])
+        pivs.append(p[0][:A.shape[0]].copy())
+        info[k], iters[k] = inf[0], it[0]
+    return Xs, pivs, info, iters
 
 
 def gesv_adjoint_batched(LU, ipiv, X, G, nthreads=None):

@@ -84,3 +84,26 @@ def test_small_path_declines_large_sizes(lib):
     # magma_?gesv_batched_small returns -100 ("not applicable") like MAGMA
     assert lib.magma_dgesv_batched_small(33, 1, None, 33, None, None, 33, None, 1, None) == -100
     assert lib.magma_dgesv_batched_small(8, 17, None, 8, None, None, 8, None, 1, None) == -100
+
+
+def test_vbatched_tuning_table_roundtrip(lib):
+    """The tuning table of the variable-size kernel: host-only get/set, validation."""
+    import ctypes as C
+    for p in "ds":
+        get = getattr(lib, f"magma_{p}vbatched_tuning_get")
+        put = getattr(lib, f"magma_{p}vbatched_tuning_set")
+        nb0, t0 = (C.c_int * 8)(), (C.c_int * 8)()
+        assert get(nb0, t0) == 0
+        assert all(x in (8, 16, 32) for x in nb0) and all(0 <= x <= 2 for x in t0)
+        nb = (C.c_int * 8)(8, 16, 32, 16, 32, 16, 32, 32)
+        tile = (C.c_int * 8)(2, 1, 0, 2, 1, 0, 2, 0)
+        assert put(nb, tile) == 0
+        nb1, t1 = (C.c_int * 8)(), (C.c_int * 8)()
+        assert get(nb1, t1) == 0
+        assert list(nb1) == list(nb) and list(t1) == list(tile)
+        assert put((C.c_int * 8)(12, 16, 32, 16, 32, 16, 32, 32), tile) == -1
+        assert put(nb, (C.c_int * 8)(0, 0, 0, 3, 0, 0, 0, 0)) == -2
+        assert put(nb0, t0) == 0                       # restore
+        # autotune argument errors need no GPU
+        assert getattr(lib, f"magma_{p}getrf_vbatched_autotune")(-1, None, None, None) == -1
+        assert getattr(lib, f"magma_{p}getrf_vbatched_autotune")(64, None, None, None) == -4

@@ -153,3 +153,42 @@ def test_dxgesv_fp32_equals_dsgesv(cuda):
     Bm = np.random.default_rng(8).uniform(-1, 1, (3, 100, 2))
     gpu, ref = _run_both(A, Bm, cuda)
     _assert_same(gpu, ref, 100)
+
+
+def _vb_case(seed, count, nmax, rmax, kappa_hi=1e6):
+    rng = np.random.default_rng(seed)
+    ns = [int(x) for x in rng.integers(1, nmax + 1, count)]
+    rs = [int(x) for x in rng.integers(1, rmax + 1, count)]
+    kap = 10.0 ** rng.uniform(0, np.log10(kappa_hi), count)
+    As, Bs = [], []
+    for k, (n, r) in enumerate(zip(ns, rs)):
+        A = _svd(1, n, [float(kap[k])], seed=seed * 1000 + k)[0]
+        As.append(np.ascontiguousarray(A.T))                     # storage (ncols, ld = n)
+        Bs.append(rng.uniform(-1, 1, (r, n)))
+    return ns, rs, As, Bs
+
+
+@pytest.mark.parametrize("tol", [0.0, 30.0])
+def test_dxgesv_vbatched_matches_oracle(cuda, tol):
+    """Variable-size refinement (FP32 persistent factorisation): solutions, pivots, info and
+    iteration counts bit-identical to the oracle matrix by matrix, including matrices with
+    kappa 1e9 that fall back to the FP64 re-solve."""
+    ns, rs, As, Bs = _vb_case(3, 40, 200, 16)
+    extra = _vb_case(4, 3, 90, 4, kappa_hi=1e10)          # some will not converge
+    ns, rs, As, Bs = ns + extra[0], rs + extra[1], As + extra[2], Bs + extra[3]
+    ns.append(1); rs.append(1); As.append(np.array([[3.0]])); Bs.append(np.array([[1.5]]))
+    A = mg.VBatch([a.shape for a in As], ns, torch.float64, cuda).load(As)
+    B = mg.VBatch([b.shape for b in Bs], ns, torch.float64, cuda).load(Bs)
+    X, ipiv, offs, info, iters = mg.dxgesv_vbatched(A, B, tol=tol)
+    torch.cuda.synchronize()
+    rA = [a.copy() for a in As]
+    rX, rp, rinfo, riters = oracle.dsgesv_vbatched(rA, Bs, tol=tol)
+    it = iters.cpu().numpy()
+    assert np.array_equal(it, riters), (it, riters)
+    assert np.array_equal(info.cpu().numpy(), rinfo)
+    P = ipiv.cpu().numpy()
+    for k, n in enumerate(ns):
+        assert np.array_equal(P[offs[k]:offs[k] + n], rp[k]), k
+        assert np.array_equal(X.view(k).cpu().numpy(), rX[k], equal_nan=True), k
+        assert np.array_equal(A.view(k).cpu().numpy(), rA[k], equal_nan=True), k
+    assert (it < 0).any() and (it >= 0).any()

@@ -183,3 +183,54 @@ def test_vbatched_argument_errors(cuda):
     assert lib.magma_dgesv_vbatched(_vp(n2), _vp(r), None, _vp(ld), None, None, _vp(n2), None, 2, q) == -4
     r2 = torch.tensor([1, -3], dtype=torch.int32, device=cuda)
     assert lib.magma_dgesv_vbatched(_vp(n2), _vp(r2), None, _vp(n2), None, None, _vp(n2), None, 2, q) == -2
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_every_tuning_choice_is_bit_exact(cuda, dtype):
+    """Each (panel width, update tile) the tuner can choose, forced on every size bin, gives
+    the oracle's factors, pivots and solutions bit for bit."""
+    rng = np.random.default_rng(21)
+    ns = [int(n) for n in rng.integers(1, 300, 24)] + [16, 17, 32, 33, 64, 65, 128, 129, 257]
+    nrhss = [int(r) for r in rng.integers(1, 17, len(ns))]
+    npdt = np.float64 if dtype == torch.float64 else np.float32
+    As, Bs = _make(rng, ns, nrhss, ld_pad=1, dtype=npdt)
+    saved = mg.vbatched_tuning(dtype)
+    try:
+        for nb in (8, 16, 32):
+            for tile in range(3):
+                mg.set_vbatched_tuning([nb] * 8, [tile] * 8, dtype)
+                gpu = _gpu_gesv(As, Bs, ns, cuda, dtype)
+                rA = [a.copy() for a in As]
+                rB = [b.copy() for b in Bs]
+                rp, rinfo = (oracle.dgesv_vbatched if dtype == torch.float64
+                             else oracle.sgesv_vbatched)(ns, nrhss, rA, rB)
+                Ao, Bo, pivs, info = gpu
+                assert np.array_equal(info, rinfo), (nb, tile)
+                for k in range(len(ns)):
+                    assert np.array_equal(pivs[k], rp[k]), (nb, tile, k)
+                    assert np.array_equal(Ao[k], rA[k], equal_nan=True), (nb, tile, k)
+                    assert np.array_equal(Bo[k], rB[k], equal_nan=True), (nb, tile, k)
+    finally:
+        mg.set_vbatched_tuning([saved[b]["nb"] for b in mg.batched.TUNE_BINS],
+                               [saved[b]["tile"] for b in mg.batched.TUNE_BINS], dtype)
+
+
+def test_autotune_installs_a_valid_table(cuda):
+    saved = mg.vbatched_tuning(torch.float64)
+    try:
+        t = mg.autotune_vbatched(96, torch.float64)
+        assert t == mg.vbatched_tuning(torch.float64)
+        for b in mg.batched.TUNE_BINS:
+            assert t[b]["nb"] in (8, 16, 32) and t[b]["tile"] in mg.batched.TILES
+        # bins above max_n keep their entries
+        for b in ("<=256", "<=512", "<=1024", ">1024"):
+            assert t[b] == saved[b]
+        # results with the tuned table still match the oracle
+        rng = np.random.default_rng(22)
+        ns = [int(n) for n in rng.integers(1, 97, 20)]
+        nrhss = [int(r) for r in rng.integers(1, 5, 20)]
+        As, Bs = _make(rng, ns, nrhss)
+        _check_same(_gpu_gesv(As, Bs, ns, cuda), As, Bs, ns, nrhss)
+    finally:
+        mg.set_vbatched_tuning([saved[b]["nb"] for b in mg.batched.TUNE_BINS],
+                               [saved[b]["tile"] for b in mg.batched.TUNE_BINS], torch.float64)
