@@ -643,8 +643,258 @@ class Adjoint2048:
         return k, statistics.median(ts), f"{k} of the {b} forward+backward solves"
 
 
+class Serve256:
+    """Serving-size workload: variable-size refinement solve plus its adjoint, one CUDA graph
+    per step (magma_dxgesv_vbatched_work + magma_dxgesv_adjoint_vbatched_work, both without
+    host synchronisation), against the plain FP64 variable-size path on the same inputs."""
+    name = "serve256"
+    batch, nrhs = 256, 8
+    seed = 20240605
+    dtype = "f64 (FP32 factorisation, FP64 residual/update; FP64-refined adjoint)"
+    itermax = 30
+    tol = 30.0
+    dominant_class = None        # graph replay; see roofline()
+    dominant = "one CUDA-graph replay: refinement forward + adjoint"
+    graph_kernels_per_step = None
+
+    def describe(self):
+        return {"workload": "256 FP64 matrices, n uniform in [128,1024], A = U diag(s) V^T (U, V "
+                            "from QR of seeded Gaussians, s geometric 1..1/kappa, kappa "
+                            "log-uniform in [1,1e4]), nrhs=8 N(0,1), upstream gradient N(0,1); "
+                            "forward: FP32 LU in the persistent variable-size kernel + FP64 "
+                            "refinement; backward: gB = A^-T gX refined in FP64 with the same FP32 "
+                            "factors, gA = -gB X^T; one CUDA graph per step",
+                "batch": self.batch, "n": "U[128,1024]", "nrhs": self.nrhs,
+                "precision": "fp32 factor, fp64 residual/update/convergence, forward and adjoint",
+                "compared_with": "magma_dgesv_vbatched + magma_dgetrs_vbatched(MagmaTrans) + "
+                                 "magmablas_dger_neg_vbatched (plain FP64) on the same inputs",
+                "tensor_core_factor": "not used: BF16/FP16 factors do not converge under plain "
+                                      "refinement for kappa up to 1e4 (kappa * u > 1)",
+                "l2": "inputs larger than L2 (A is ~0.8 GB FP64)"}
+
+    def sizes(self):
+        rng = np.random.default_rng(self.seed)
+        ns = [int(x) for x in rng.integers(128, 1025, self.batch)]
+        kap = [float(x) for x in 10.0 ** rng.uniform(0.0, 4.0, self.batch)]
+        return ns, kap
+
+    def host_inputs(self):
+        ns, kap = self.sizes()
+        As, Bs, Gs = [], [], []
+        for k, (n, kp) in enumerate(zip(ns, kap)):
+            rng = np.random.default_rng(self.seed * 7919 + k)
+            U = np.linalg.qr(rng.standard_normal((n, n)))[0]
+            V = np.linalg.qr(rng.standard_normal((n, n)))[0]
+            sv = np.geomspace(1.0, 1.0 / kp, n)
+            As.append(np.ascontiguousarray(((U * sv) @ V.T).T))       # storage (ncols, ld=n)
+            Bs.append(rng.standard_normal((self.nrhs, n)))
+            Gs.append(rng.standard_normal((self.nrhs, n)))
+        return ns, As, Bs, Gs
+
+    def flops(self):
+        ns, _ = self.sizes()
+        return sum(flops_getrf(n, n) for n in ns)
+
+    def _calls(self, c, q):
+        lib, b = c["lib"], self.batch
+        A, B, X, G, GB, GA = c["A"], c["B"], c["X"], c["G"], c["GB"], c["GA"]
+        rc = lib.magma_dxgesv_vbatched_work(
+            900, vp(A.ncols), vp(B.ncols), c["max_n"], self.nrhs, vp(A.ptrs), vp(A.ld),
+            vp(c["dP"]), vp(B.ptrs), vp(B.ld), vp(X.ptrs), vp(X.ld), vp(c["info"]),
+            vp(c["iter"]), self.itermax, self.tol, 0, vp(c["work"]), C.byref(c["lwork"]), b,
+            q.handle)
+        if rc != 0:
+            raise RuntimeError(f"magma_dxgesv_vbatched_work returned {rc}")
+        rc = lib.magma_dxgesv_adjoint_vbatched_work(
+            vp(A.ncols), vp(G.ncols), c["max_n"], self.nrhs, vp(A.ptrs), vp(A.ld), vp(c["dP"]),
+            vp(X.ptrs), vp(X.ld), vp(G.ptrs), vp(G.ld), vp(GB.ptrs), vp(GB.ld), vp(GA.ptrs),
+            vp(GA.ld), vp(c["iter"]), vp(c["info"]), vp(c["iter_adj"]), self.itermax, self.tol, 0,
+            vp(c["work"]), c["lwork"].value, b, q.handle)
+        if rc != 0:
+            raise RuntimeError(f"magma_dxgesv_adjoint_vbatched_work returned {rc}")
+
+    def setup(self, dev, nsteps, lib, q):
+        import torch
+        from magma_gb300.batched import VBatch, Queue
+        ns, As, Bs, Gs = self.host_inputs()
+        c = {"ns": ns, "As": As, "Bs": Bs, "Gs": Gs, "lib": lib, "max_n": max(ns)}
+        c["A"] = VBatch([a.shape for a in As], ns, torch.float64, dev).load(As)
+        c["B"] = VBatch([b.shape for b in Bs], ns, torch.float64, dev).load(Bs)
+        c["G"] = VBatch([g.shape for g in Gs], ns, torch.float64, dev).load(Gs)
+        c["X"] = VBatch(c["B"].shapes, ns, torch.float64, dev)
+        c["GB"] = VBatch(c["G"].shapes, ns, torch.float64, dev)
+        c["GA"] = VBatch([(n, n) for n in ns], ns, torch.float64, dev)
+        offs = np.concatenate([[0], np.cumsum(ns)[:-1]])
+        c["ipiv"] = torch.zeros((sum(ns),), dtype=torch.int32, device=dev)
+        c["dP"] = c["ipiv"].data_ptr() + torch.tensor(offs, dtype=torch.int64, device=dev) * 4
+        b = self.batch
+        c["info"] = torch.empty((b,), dtype=torch.int32, device=dev)
+        c["iter"] = torch.empty((b,), dtype=torch.int32, device=dev)
+        c["iter_adj"] = torch.empty((b,), dtype=torch.int32, device=dev)
+        lw = C.c_size_t(0)
+        rc = lib.magma_dxgesv_vbatched_work(900, None, None, c["max_n"], self.nrhs, None, None,
+                                            None, None, None, None, None, None, None,
+                                            self.itermax, self.tol, 0, None, C.byref(lw), b, None)
+        if rc != 0:
+            raise RuntimeError(f"workspace query returned {rc}")
+        c["work"] = torch.empty((lw.value,), dtype=torch.uint8, device=dev)
+        c["lwork"] = C.c_size_t(lw.value)
+        stream = torch.cuda.Stream(dev)
+        c["gq"] = Queue(dev.index, stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        with torch.cuda.stream(stream):
+            self._calls(c, c["gq"])               # eager once (kernel attributes)
+            stream.synchronize()
+            n0 = lib.magma_lu_launch_count()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                self._calls(c, c["gq"])
+            self.graph_kernels_per_step = lib.magma_lu_launch_count() - n0
+        c["graph"] = g
+        torch.cuda.synchronize(dev)
+        return c
+
+    def step(self, c, i):
+        c["graph"].replay()
+
+    def e2e_setup(self, c):
+        import torch
+        c["hA"] = c["A"].buf.cpu().pin_memory()
+        c["hB"] = c["B"].buf.cpu().pin_memory()
+        c["hG"] = c["G"].buf.cpu().pin_memory()
+        c["hX"] = torch.empty_like(c["X"].buf, device="cpu").pin_memory()
+        c["hGB"] = torch.empty_like(c["GB"].buf, device="cpu").pin_memory()
+        c["hGA"] = torch.empty_like(c["GA"].buf, device="cpu").pin_memory()
+        h2d = (c["hA"].numel() + c["hB"].numel() + c["hG"].numel()) * 8
+        d2h = (c["hX"].numel() + c["hGB"].numel() + c["hGA"].numel()) * 8
+        return h2d, d2h
+
+    def e2e_step(self, c):
+        c["A"].buf.copy_(c["hA"], non_blocking=True)
+        c["B"].buf.copy_(c["hB"], non_blocking=True)
+        c["G"].buf.copy_(c["hG"], non_blocking=True)
+        c["graph"].replay()
+        c["hX"].copy_(c["X"].buf, non_blocking=True)
+        c["hGB"].copy_(c["GB"].buf, non_blocking=True)
+        c["hGA"].copy_(c["GA"].buf, non_blocking=True)
+
+    def accuracy(self, c, last):
+        """Forward scaled residual ||B - A X|| / (||A|| ||X|| n eps) and adjoint scaled residual
+        ||G - A^T GB|| / (||A^T|| ||GB|| n eps); a solve counts when both are <= 30."""
+        import torch
+        ok, worst_f, worst_b = 0, 0.0, 0.0
+        dev = c["A"].buf.device
+        for k, n in enumerate(c["ns"]):
+            A = torch.from_numpy(c["As"][k]).to(dev).T          # math orientation
+            X = c["X"].view(k).T
+            B = torch.from_numpy(c["Bs"][k]).to(dev).T
+            GB = c["GB"].view(k).T
+            G = torch.from_numpy(c["Gs"][k]).to(dev).T
+            rf = float(scaled_residuals(A[None], X[None], B[None])[0])
+            rb = float(scaled_residuals(A.T[None], GB[None], G[None])[0])
+            worst_f, worst_b = max(worst_f, rf), max(worst_b, rb)
+            ok += rf <= 30 and rb <= 30
+        it = c["iter"].cpu().numpy()
+        ia = c["iter_adj"].cpu().numpy()
+        return ok, max(worst_f, worst_b), {
+            "max_scaled_residual_forward": worst_f, "max_scaled_residual_adjoint": worst_b,
+            "iterations_forward": {str(int(k)): int(v) for k, v in zip(*np.unique(it, return_counts=True))},
+            "iterations_adjoint": {str(int(k)): int(v) for k, v in zip(*np.unique(ia, return_counts=True))}}
+
+    def fp64_path(self, c, steps, warmup):
+        """Plain FP64: magma_dgesv_vbatched, then magma_dgetrs_vbatched(MagmaTrans) with its
+        factors and magmablas_dger_neg_vbatched, on private copies of the same inputs."""
+        import torch
+        from magma_gb300.batched import VBatch, Queue
+        lib, b, ns = c["lib"], self.batch, c["ns"]
+        dev = c["A"].buf.device
+        q = Queue.current(dev)
+        stream = torch.cuda.current_stream(dev)
+        A = VBatch(c["A"].shapes, ns, torch.float64, dev)
+        X = VBatch(c["B"].shapes, ns, torch.float64, dev)
+        GB = VBatch(c["G"].shapes, ns, torch.float64, dev)
+        GA = VBatch(c["GA"].shapes, ns, torch.float64, dev)
+        ipiv = torch.zeros((sum(ns),), dtype=torch.int32, device=dev)
+        offs = np.concatenate([[0], np.cumsum(ns)[:-1]])
+        dP = ipiv.data_ptr() + torch.tensor(offs, dtype=torch.int64, device=dev) * 4
+        info = torch.empty((b,), dtype=torch.int32, device=dev)
+
+        def call():
+            A.buf.copy_(c["A"].buf)
+            X.buf.copy_(c["B"].buf)
+            GB.buf.copy_(c["G"].buf)
+            rc = lib.magma_dgesv_vbatched(vp(A.ncols), vp(X.ncols), vp(A.ptrs), vp(A.ld), vp(dP),
+                                          vp(X.ptrs), vp(X.ld), vp(info), b, q.handle)
+            rc = rc or lib.magma_dgetrs_vbatched(112, vp(A.ncols), vp(GB.ncols), vp(A.ptrs),
+                                                 vp(A.ld), vp(dP), vp(GB.ptrs), vp(GB.ld), b,
+                                                 q.handle)
+            rc = rc or lib.magmablas_dger_neg_vbatched(vp(A.ncols), vp(GB.ncols), c["max_n"],
+                                                       vp(GB.ptrs), vp(GB.ld), vp(X.ptrs),
+                                                       vp(X.ld), vp(GA.ptrs), vp(GA.ld), b,
+                                                       q.handle)
+            if rc != 0:
+                raise RuntimeError(f"plain FP64 variable-size path returned {rc}")
+        for _ in range(warmup):
+            call()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        ok = 0
+        for k in range(b):
+            Am = torch.from_numpy(c["As"][k]).to(dev).T
+            rf = float(scaled_residuals(Am[None], X.view(k).T[None],
+                                        torch.from_numpy(c["Bs"][k]).to(dev).T[None])[0])
+            rb = float(scaled_residuals(Am.T[None], GB.view(k).T[None],
+                                        torch.from_numpy(c["Gs"][k]).to(dev).T[None])[0])
+            ok += rf <= 30 and rb <= 30
+        return {"value": ok / (ms * 1e-3), "unit": "solves/s", "ms_per_step": ms, "steps": steps,
+                "note": "includes restoring the inputs (three device copies) each step",
+                "call": "magma_dgesv_vbatched + magma_dgetrs_vbatched(MagmaTrans) + "
+                        "magmablas_dger_neg_vbatched"}
+
+    def roofline(self, kern, peaks, c):
+        # the step is one graph replay; its FP32 factorisation (2/3 n^3 per matrix) is the
+        # largest block of work, reported against the FP32 FMA rate, and the FP64 residual
+        # passes against the FP64 rate
+        import torch
+        ms = kern["launch_ms"]
+        flops = self.flops()
+        ach = flops / (ms * 1e-3) / 1e12
+        return {"bound": "fp32", "achieved": ach, "peak": peaks["fp32_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["fp32_tflops"], "traffic": None, **kern,
+                "kernel": "one CUDA-graph replay (factorisation flops / replay time)",
+                "algorithmic_flops_per_launch": flops,
+                "peak_source": "FP32 FMA-throughput probe run inside bench.py"}
+
+    def cpu_sample(self, nthreads, target_s):
+        import oracle
+        ns, As, Bs, Gs = self.host_inputs() if not hasattr(self, "_host") else self._host
+        self._host = (ns, As, Bs, Gs)
+
+        def run(k):
+            a = [x.copy() for x in As[:k]]
+            b = [x.copy() for x in Bs[:k]]
+            t0 = time.perf_counter()
+            pivs, _ = oracle.dgesv_vbatched(ns[:k], [self.nrhs] * k, a, b, nthreads=nthreads)
+            for j in range(k):
+                oracle.gesv_adjoint_batched(a[j][None], pivs[j][None], b[j][None],
+                                            Gs[j][None].copy(), nthreads=1)
+            return time.perf_counter() - t0
+        k = 16
+        t = run(k)
+        k = int(min(self.batch, max(k, k * target_s / max(t, 1e-6))))
+        ts = [run(k) for _ in range(3)]
+        return k, statistics.median(ts), f"the first {k} of the {self.batch} matrices (FP64 " \
+                                         f"dgetrf + dgetrs + transposed dgetrs + outer product)"
+
+
 WORKLOADS = {"dsgesv512": Dsgesv512, "gesv32": Gesv32, "vbatched4096": GesvVbatched,
-             "adjoint2048": Adjoint2048}
+             "adjoint2048": Adjoint2048, "serve256": Serve256}
 
 
 # DRAM bytes (read + write) per unit of work of each workload's dominant kernel, from the ncu

@@ -454,6 +454,56 @@ magma_int_t magma_dxgesv_vbatched_work(magma_int_t precision, magma_int_t *n, ma
                                        void *work, size_t *lwork, magma_int_t batchCount,
                                        magma_queue_t queue);
 
+/* No counterpart in the reference: the adjoint of a refinement solve.  Given
+ * the forward call's inputs and outputs -- A and ipiv as magma_dxgesv_batched_work
+ * (precision 900) or magma_dxgesv_vbatched_work left them, its solution X, its
+ * iteration codes diter_fwd and its workspace `work` (same sizes, untouched
+ * since, holding the FP32 factors) -- and an upstream gradient G of X, computes
+ * GB = A^{-T} G (the gradient of B), refined to FP64 accuracy with the FP32
+ * factors (residual G - A^T GB in FP64, the forward's stopping rule with
+ * ||A^T||_inf), and, when dGA_array is not NULL, GA = -GB X^T (the gradient of
+ * A).  Matrices whose forward solve fell back to FP64 use their FP64 factors
+ * (a transposed FP64 solve); with `fallback`, matrices whose adjoint
+ * refinement does not converge are factored in FP64 in place (A, ipiv and
+ * info overwritten) and solved the same way.  diter_array receives the
+ * adjoint's iteration codes (the forward's code for FP64 matrices).  G is not
+ * modified.  With `fallback` the call synchronises once (to size the FP64
+ * solves); without it, it never synchronises (capturable in a CUDA graph) and
+ * matrices with a negative forward or adjoint code keep an unsolved GB.  Errors: negative
+ * argument positions; MAGMA_ERR_NOT_SUPPORTED for orders whose solve or
+ * residual does not fit in shared memory. */
+magma_int_t magma_dxgesv_adjoint_batched_work(magma_int_t n, magma_int_t nrhs, double **dA_array,
+                                              magma_int_t ldda, magma_int_t **dipiv_array,
+                                              double **dX_array, magma_int_t lddx,
+                                              double **dG_array, magma_int_t lddg,
+                                              double **dGB_array, magma_int_t lddgb,
+                                              double **dGA_array, magma_int_t lddga,
+                                              magma_int_t *diter_fwd, magma_int_t *dinfo_array,
+                                              magma_int_t *diter_array, magma_int_t itermax,
+                                              double tol, magma_int_t fallback, void *work,
+                                              size_t lwork, magma_int_t batchCount,
+                                              magma_queue_t queue);
+magma_int_t magma_dxgesv_adjoint_vbatched_work(magma_int_t *n, magma_int_t *nrhs,
+                                               magma_int_t max_n, magma_int_t max_nrhs,
+                                               double **dA_array, magma_int_t *ldda,
+                                               magma_int_t **dipiv_array, double **dX_array,
+                                               magma_int_t *lddx, double **dG_array,
+                                               magma_int_t *lddg, double **dGB_array,
+                                               magma_int_t *lddgb, double **dGA_array,
+                                               magma_int_t *lddga, magma_int_t *diter_fwd,
+                                               magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                               magma_int_t itermax, double tol,
+                                               magma_int_t fallback, void *work, size_t lwork,
+                                               magma_int_t batchCount, magma_queue_t queue);
+
+/* No counterpart in the reference: magmablas_dger_neg_batched for a
+ * variable-size batch, GA_k = -G_k X_k^T (order n[k], nrhs[k] columns; max_n
+ * the largest order).  Errors: -3 max_n, -10 batchCount. */
+magma_int_t magmablas_dger_neg_vbatched(magma_int_t *n, magma_int_t *nrhs, magma_int_t max_n,
+                                        double **dG_array, magma_int_t *lddg, double **dX_array,
+                                        magma_int_t *lddx, double **dGA_array, magma_int_t *lddga,
+                                        magma_int_t batchCount, magma_queue_t queue);
+
 /* ------------------------------------------------------------------------
  * Tuning of the variable-size kernel.  No counterpart in the reference, whose
  * batched routines read fixed crossover tables
@@ -466,8 +516,12 @@ magma_int_t magma_dxgesv_vbatched_work(magma_int_t precision, magma_int_t *n, ma
  * choice changes a result bit: every element receives the same updates in the
  * same order.
  *
+ * Batches whose largest matrix exceeds 256 do not use the table: they run the
+ * per-step kernels of the fixed-size path with per-matrix sizes (several CTAs
+ * per matrix and step).
+ *
  * magma_?getrf_vbatched_autotune: times every (nb in {16, 32}) x (tile)
- * candidate on `queue`'s device for each bin up to max_n (bins above 1024 are
+ * candidate on `queue`'s device for each bin up to max_n (bins above 256 are
  * not timed), installs the fastest in the table of that precision and returns
  * the table in nb[8], tile[8] (either may be NULL).  Allocates its trial
  * batches and synchronises the queue.  max_n = 0 only returns the table.

@@ -279,7 +279,8 @@ def dxgesv_vbatched(A: "VBatch", B: "VBatch", X: "VBatch | None" = None, precisi
     """Mixed-precision refinement of a variable-size FP64 batch
     (magma_dxgesv_vbatched_work).  A is left intact except for matrices that fall back
     to the FP64 re-solve; B is read; X (allocated like B when None) receives the solutions.
-    Returns (X, ipiv buffer, per-matrix ipiv offsets, info, iters)."""
+    Returns (X, ipiv buffer, per-matrix ipiv offsets, info, iters, work); keep `work` (it
+    holds the FP32 factors) for dxgesv_adjoint_vbatched."""
     if A.buf.dtype != torch.float64:
         raise TypeError("dxgesv_vbatched expects float64 batches")
     b = len(A.shapes)
@@ -315,7 +316,57 @@ def dxgesv_vbatched(A: "VBatch", B: "VBatch", X: "VBatch | None" = None, precisi
                                         itermax, float(tol), int(fallback), _vp(work),
                                         C.byref(lw), b, q.handle)
     _check(rc, "magma_dxgesv_vbatched_work")
-    return X, ipiv, offs, info, iters
+    return X, ipiv, offs, info, iters, work
+
+
+def dsgesv_adjoint_batched(S: torch.Tensor, ipiv: torch.Tensor, X: torch.Tensor, G: torch.Tensor,
+                           iters_fwd: torch.Tensor, work: torch.Tensor, info: torch.Tensor,
+                           itermax: int = 30, tol: float = 0.0, fallback: bool = True,
+                           want_ga: bool = True, queue: Queue | None = None):
+    """Adjoint of dsgesv_batched (magma_dxgesv_adjoint_batched_work): S, ipiv, X, iters_fwd,
+    info and `work` as the forward call left them, G the upstream gradient of X (storage like
+    X).  Returns (GB, GA, iters): GB = A^{-T} G (storage like G), GA = -GB X^T
+    ((batch, n, n) storage) or None."""
+    b, n, ld = S.shape
+    nrhs = X.shape[1]
+    GB = torch.empty_like(G)
+    GA = torch.empty((b, n, n), dtype=torch.float64, device=S.device) if want_ga else None
+    iters = torch.empty((b,), dtype=torch.int32, device=S.device)
+    q = queue or Queue.current(S.device)
+    dA, dP, dX, dG, dGB = ptr_array(S), ptr_array(ipiv), ptr_array(X), ptr_array(G), ptr_array(GB)
+    dGA = ptr_array(GA) if want_ga else None
+    rc = _L.load().magma_dxgesv_adjoint_batched_work(
+        n, nrhs, _vp(dA), ld, _vp(dP), _vp(dX), X.shape[2], _vp(dG), G.shape[2], _vp(dGB),
+        GB.shape[2], _vp(dGA) if want_ga else None, n, _vp(iters_fwd), _vp(info), _vp(iters),
+        itermax, float(tol), int(fallback), _vp(work), work.numel(), b, q.handle)
+    _check(rc, "magma_dxgesv_adjoint_batched_work")
+    return GB, GA, iters
+
+
+def dxgesv_adjoint_vbatched(A: "VBatch", ipiv: torch.Tensor, offs, X: "VBatch", G: "VBatch",
+                            iters_fwd: torch.Tensor, info: torch.Tensor, work: torch.Tensor,
+                            itermax: int = 30, tol: float = 0.0, fallback: bool = True,
+                            want_ga: bool = True, queue: Queue | None = None):
+    """Adjoint of dxgesv_vbatched (magma_dxgesv_adjoint_vbatched_work).  Returns
+    (GB, GA, iters) with GB a VBatch like G and GA a VBatch of (n_k, n_k) matrices or None."""
+    b = len(A.shapes)
+    dev = A.buf.device
+    GB = VBatch(G.shapes, G.nrows, torch.float64, dev)
+    GA = VBatch([(s[0], s[0]) for s in A.shapes], [s[0] for s in A.shapes], torch.float64,
+                dev) if want_ga else None
+    iters = torch.empty((b,), dtype=torch.int32, device=dev)
+    max_n = max([s[0] for s in A.shapes] + [0])
+    max_r = max([s[0] for s in G.shapes] + [0])
+    dP = ipiv.data_ptr() + torch.tensor(offs, dtype=torch.int64, device=dev) * 4
+    q = queue or Queue.current(dev)
+    rc = _L.load().magma_dxgesv_adjoint_vbatched_work(
+        _vp(A.ncols), _vp(G.ncols), max_n, max_r, _vp(A.ptrs), _vp(A.ld), _vp(dP), _vp(X.ptrs),
+        _vp(X.ld), _vp(G.ptrs), _vp(G.ld), _vp(GB.ptrs), _vp(GB.ld),
+        _vp(GA.ptrs) if want_ga else None, _vp(GA.ld) if want_ga else None, _vp(iters_fwd),
+        _vp(info), _vp(iters), itermax, float(tol), int(fallback), _vp(work), work.numel(), b,
+        q.handle)
+    _check(rc, "magma_dxgesv_adjoint_vbatched_work")
+    return GB, GA, iters
 
 
 # --------------------------------------------------------------------------

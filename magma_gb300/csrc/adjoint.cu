@@ -27,12 +27,21 @@ constexpr int GER_TILE = 64, GER_RMAX = 16;
 template <typename T>
 __global__ void __launch_bounds__(256)
 ger_neg_kernel(int n, int nrhs, T **dG_array, int lddg, T **dX_array, int lddx, T **dGA_array,
-               int lddga, int tiles)
+               int lddga, int tiles, const int *n_arr, const int *nrhs_arr, const int *lddg_arr,
+               const int *lddx_arr, const int *lddga_arr)
 {
     __shared__ T sG[GER_RMAX][GER_TILE], sX[GER_RMAX][GER_TILE];
     const int mat = blockIdx.y;
     const int ti = blockIdx.x % tiles, tj = blockIdx.x / tiles;
     const int i0 = ti * GER_TILE, j0 = tj * GER_TILE;
+    if (n_arr) {                      // variable sizes: this matrix's own
+        n = n_arr[mat];
+        nrhs = nrhs_arr[mat];
+        lddg = lddg_arr[mat];
+        lddx = lddx_arr[mat];
+        lddga = lddga_arr[mat];
+        if (i0 >= n || j0 >= n) return;
+    }
     const T *G = dG_array[mat];
     const T *X = dX_array[mat];
     T *GA = dGA_array[mat];
@@ -85,7 +94,8 @@ magma_int_t ger_neg(int n, int nrhs, T **dG, int lddg, T **dX, int lddx, T **dGA
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
         MLU_LAUNCH(mlu::KC_ADJ_GER, q->stream, ger_neg_kernel<T><<<dim3(tiles * tiles, nb), 256, 0, q->stream>>>(
-            n, nrhs, dG + b0, lddg, dX + b0, lddx, dGA + b0, lddga, tiles));
+            n, nrhs, dG + b0, lddg, dX + b0, lddx, dGA + b0, lddga, tiles, nullptr, nullptr,
+            nullptr, nullptr, nullptr));
     }
     MLU_CHECK_LAUNCH();
     return 0;
@@ -182,4 +192,44 @@ extern "C" magma_int_t magma_sgesv_adjoint_batched(magma_int_t n, magma_int_t nr
 {
     return adjoint_entry<float>(__func__, n, nrhs, dLU_array, ldda, dipiv_array, dX_array, lddx,
                                 dG_array, lddg, dGA_array, lddga, batchCount, queue);
+}
+
+// ---------------------------------------------------------------------------
+// Variable sizes (no counterpart in the reference): GA_k = -G_k X_k^T for
+// matrices of order n[k] with nrhs[k] columns; max_n is the largest n[k].
+
+namespace mlu {
+template <typename T>
+magma_int_t ger_neg_vbatched(const int *n, const int *nrhs, int max_n, T **dG, const int *lddg,
+                             T **dX, const int *lddx, T **dGA, const int *lddga, int batch,
+                             magma_queue_t q)
+{
+    if (max_n <= 0 || batch <= 0) return 0;
+    const int tiles = (max_n + GER_TILE - 1) / GER_TILE;
+    for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
+        const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
+        MLU_LAUNCH(mlu::KC_ADJ_GER, q->stream,
+                   ger_neg_kernel<T><<<dim3(tiles * tiles, nb), 256, 0, q->stream>>>(
+                       max_n, 0, dG + b0, 1, dX + b0, 1, dGA + b0, 1, tiles, n + b0, nrhs + b0,
+                       lddg + b0, lddx + b0, lddga + b0));
+    }
+    MLU_CHECK_LAUNCH();
+    return 0;
+}
+template magma_int_t ger_neg_vbatched<double>(const int *, const int *, int, double **, const int *,
+                                              double **, const int *, double **, const int *, int,
+                                              magma_queue_t);
+}  // namespace mlu
+
+extern "C" magma_int_t magmablas_dger_neg_vbatched(magma_int_t *n, magma_int_t *nrhs,
+                                                   magma_int_t max_n, double **dG_array,
+                                                   magma_int_t *lddg, double **dX_array,
+                                                   magma_int_t *lddx, double **dGA_array,
+                                                   magma_int_t *lddga, magma_int_t batchCount,
+                                                   magma_queue_t queue)
+{
+    if (max_n < 0) return -3;
+    if (batchCount < 0) return -10;
+    return mlu::ger_neg_vbatched<double>(n, nrhs, max_n, dG_array, lddg, dX_array, lddx,
+                                         dGA_array, lddga, batchCount, queue);
 }

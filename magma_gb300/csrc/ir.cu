@@ -41,7 +41,30 @@ magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int m
                    T **dA, const int *ldda, int **ipiv, T **dB, const int *lddb, int *info,
                    void *work, int batch, magma_queue_t q, const VbTune *tune_override);
 size_t vb_work_bytes(int batch);
+template <typename T>
+magma_int_t vb_getrs_run(bool trans, const int *n, const int *nrhs, int max_n, int max_nrhs, T **dA,
+                         const int *ldda, int **ipiv, T **dB, const int *lddb, int batch,
+                         magma_queue_t q);
+template <typename T>
+magma_int_t ger_neg_vbatched(const int *n, const int *nrhs, int max_n, T **dG, const int *lddg,
+                             T **dX, const int *lddx, T **dGA, const int *lddga, int batch,
+                             magma_queue_t q);
 }  // namespace mlu
+
+extern "C" magma_int_t magma_dgetrf_batched(magma_int_t m, magma_int_t n, double **dA_array,
+                                            magma_int_t ldda, magma_int_t **ipiv_array,
+                                            magma_int_t *info_array, magma_int_t batchCount,
+                                            magma_queue_t queue);
+extern "C" magma_int_t magma_dgetrs_batched(magma_trans_t trans, magma_int_t n, magma_int_t nrhs,
+                                            double **dA_array, magma_int_t ldda,
+                                            magma_int_t **dipiv_array, double **dB_array,
+                                            magma_int_t lddb, magma_int_t batchCount,
+                                            magma_queue_t queue);
+extern "C" magma_int_t magmablas_dger_neg_batched(magma_int_t n, magma_int_t nrhs,
+                                                  double **dG_array, magma_int_t lddg,
+                                                  double **dX_array, magma_int_t lddx,
+                                                  double **dGA_array, magma_int_t lddga,
+                                                  magma_int_t batchCount, magma_queue_t queue);
 
 extern "C" magma_int_t magma_sgetrf_batched(magma_int_t m, magma_int_t n, float **dA_array,
                                             magma_int_t ldda, magma_int_t **ipiv_array,
@@ -66,6 +89,7 @@ constexpr int IR_ROWS = 128;       // rows per CTA in the FP64 kernels
 constexpr int IR_NRHS_MAX = 16;
 constexpr int IR_SOLVE_NR = 8;
 constexpr int IR_ACTIVE = 0, IR_CONVERGED = 1, IR_FAILED = 2;
+constexpr int IR_FP64 = 3;   // adjoint: the forward solve fell back, A holds FP64 factors
 
 // per-matrix statistics block (8-byte words)
 //   [0] anorm bits  [1] state  [2 + par*(2*NRMAX+2) + ...] norms for parity par:
@@ -238,7 +262,7 @@ __device__ __forceinline__ bool ir_converged(const unsigned long long *st, int p
 
 // check (when it >= 0) + correction solve X += float-solve(R) with the FP32
 // factors.  One CTA per (matrix, group of NR right-hand sides).
-template <int NR>
+template <int NR, bool TRANS>
 __global__ void __launch_bounds__(256)
 ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double **dX_array,
                 const double *R, unsigned long long *stats, int *iter, const int *info, int it,
@@ -253,7 +277,7 @@ ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double
     unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
     if (tid == 0) {
         int go = st[1] == IR_ACTIVE;
-        if (go && it < 0 && info[mat] > 0) {          // FP32 factorisation hit a zero pivot
+        if (go && it < 0 && info != nullptr && info[mat] > 0) {   // FP32 factor hit a zero pivot
             go = 0;
             if (blockIdx.x == 0) { st[1] = IR_FAILED; iter[mat] = -3; }
         }
@@ -274,21 +298,111 @@ ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double
     const int nr = min(NR, nrhs - c0);
     const double *Rm = R + ((size_t)mat * sh.nrhs + c0) * sh.n;
     const int *pm = perm + (size_t)mat * sh.n;
-    // row interchanges applied while loading: sB[i] = R[perm[i]]
-    for (int e = tid; e < NR * n; e += blockDim.x) {
-        const int c = e / n, i = e % n;
-        const int p = pm[i];
-        const double rv = c < nr ? Rm[p + (size_t)c * sh.n] : 0.0;
-        sB[c * n + i] = __double2float_rn(rowscale ? rv * rowscale[(size_t)mat * sh.n + p] : rv);
+    if (!TRANS) {
+        // row interchanges applied while loading: sB[i] = R[perm[i]]
+        for (int e = tid; e < NR * n; e += blockDim.x) {
+            const int c = e / n, i = e % n;
+            const int p = pm[i];
+            const double rv = c < nr ? Rm[p + (size_t)c * sh.n] : 0.0;
+            sB[c * n + i] = __double2float_rn(rowscale ? rv * rowscale[(size_t)mat * sh.n + p] : rv);
+        }
+    } else {
+        for (int e = tid; e < NR * n; e += blockDim.x) {
+            const int c = e / n, i = e % n;
+            sB[c * n + i] = __double2float_rn(c < nr ? Rm[i + (size_t)c * sh.n] : 0.0);
+        }
     }
     __syncthreads();
-    solve_smem<float, false, NR>(n, dAs_array[mat], ldas, nullptr, sB, nr);
+    solve_smem<float, TRANS, NR>(n, dAs_array[mat], ldas, nullptr, sB, nr);
     double *X = dX_array[mat] + (size_t)c0 * lddx;
     for (int e = tid; e < nr * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
         const double d = (double)sB[c * n + i];
-        X[i + (size_t)c * lddx] = X[i + (size_t)c * lddx] +
+        // A^T: the interchanges undone on the way out, x[perm[i]] += w[i]
+        const int r = TRANS ? pm[i] : i;
+        X[r + (size_t)c * lddx] = X[r + (size_t)c * lddx] +
                                   (colscale ? d * colscale[(size_t)mat * sh.n + i] : d);
+    }
+}
+
+// Adjoint refinement (A^T GB = G with the forward's FP32 factors): ||A^T||_inf
+// as the FP32 column sums of |float(a_ij)| (i ascending), R = G, GB = 0.
+// Matrices whose forward solve fell back to FP64 (iter_fwd < 0) are marked
+// IR_FP64 and solved afterwards with their FP64 factors.
+__global__ void __launch_bounds__(IR_ROWS)
+ir_init_adj_kernel(IrShape sh, double **dA_array, double **dG_array, double **dGB_array,
+                   double *R, unsigned long long *stats, const int *iter_fwd, int *iter)
+{
+    const int mat = blockIdx.y;
+    const int n = sh.N(mat), nrhs = sh.NR(mat);
+    const int ldda = sh.LDA(mat), ldg = sh.LDB(mat), ldgb = sh.LDX(mat);
+    unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
+    if (n == 0 || nrhs == 0 || iter_fwd[mat] < 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            const bool empty = n == 0 || nrhs == 0;
+            st[1] = empty ? IR_CONVERGED : IR_FP64;
+            iter[mat] = empty ? 0 : iter_fwd[mat];
+        }
+        return;
+    }
+    if (blockIdx.x * IR_ROWS >= n) return;
+    const int j = blockIdx.x * IR_ROWS + threadIdx.x;
+    float cs = 0.f;
+    if (j < n) {
+        const double *A = dA_array[mat] + (size_t)j * ldda;
+        for (int i = 0; i < n; i++) cs += fabsf(d2f_rn_int(A[i]));
+        const double *G = dG_array[mat];
+        double *GB = dGB_array[mat];
+        double *Rm = R + (size_t)mat * sh.nrhs * sh.n;
+        for (int c = 0; c < nrhs; c++) {
+            Rm[j + (size_t)c * sh.n] = G[j + (size_t)c * ldg];
+            GB[j + (size_t)c * ldgb] = 0.0;
+        }
+    }
+    atomic_max_nonneg(&st[0], j < n ? (double)cs : 0.0);
+}
+
+// Gathers the matrices the adjoint refinement did not solve: list 1 all of them
+// (GB restarted from G for an FP64 transposed solve), list 2 those whose A
+// still needs its FP64 factorisation (the refinement did not converge).
+__global__ void ir_compact_adj_kernel(IrShape sh, double **dA_array, int **ipiv_array,
+                                      double **dG_array, double **dGB_array,
+                                      const unsigned long long *stats, int batch, int *counters,
+                                      double **cA, int **cP, double **cGB, int *csize,
+                                      double **cA2, int **cP2, int *cidx2, int *csize2)
+{
+    const int mat = blockIdx.x;
+    const unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
+    const unsigned long long state = st[1];
+    if (state != IR_FAILED && state != IR_FP64) return;
+    const int n = sh.N(mat), nrhs = sh.NR(mat), ldg = sh.LDB(mat), ldgb = sh.LDX(mat);
+    if (threadIdx.x == 0) {
+        const int s1 = atomicAdd(&counters[0], 1);
+        cA[s1] = dA_array[mat];
+        cP[s1] = ipiv_array[mat];
+        cGB[s1] = dGB_array[mat];
+        if (csize) {
+            csize[s1] = n;
+            csize[batch + s1] = nrhs;
+            csize[2 * batch + s1] = sh.LDA(mat);
+            csize[3 * batch + s1] = ldgb;
+        }
+        if (state == IR_FAILED) {
+            const int s2 = atomicAdd(&counters[1], 1);
+            cA2[s2] = dA_array[mat];
+            cP2[s2] = ipiv_array[mat];
+            cidx2[s2] = mat;
+            if (csize2) {
+                csize2[s2] = n;
+                csize2[batch + s2] = sh.LDA(mat);
+            }
+        }
+    }
+    const double *G = dG_array[mat];
+    double *GB = dGB_array[mat];
+    for (int e = threadIdx.x; e < n * nrhs; e += blockDim.x) {
+        const int c = e / n, i = e % n;
+        GB[i + (size_t)c * ldgb] = G[i + (size_t)c * ldg];
     }
 }
 
@@ -315,8 +429,9 @@ __global__ void ir_perm_kernel(IrShape sh, int **ipiv_array, int *perm)
 }
 
 // R = B - A X in FP64 (acc = b_i, then acc = fma(-a_ij, x_j, acc) for j = 0..n-1),
-// with the column and row-sum infinity norms of R and X.
-template <int NR>
+// or R = B - A^T X (a_ji in place of a_ij), with the column and row-sum
+// infinity norms of R and X.
+template <int NR, bool TRANS>
 __global__ void __launch_bounds__(IR_ROWS)
 ir_residual_kernel(IrShape sh, double **dA_array, double **dB_array, double **dX_array, double *R,
                    unsigned long long *stats, int par)
@@ -342,9 +457,11 @@ ir_residual_kernel(IrShape sh, double **dA_array, double **dB_array, double **dX
     if (i < n) {
 #pragma unroll
         for (int c = 0; c < NR; c++) acc[c] = c < nrhs ? B[i + (size_t)c * lddb] : 0.0;
-        const double *Ai = A + i;
+        // row i of A, or row i of A^T (column i of A, contiguous)
+        const double *Ai = TRANS ? A + (size_t)i * ldda : A + i;
+        const size_t step = TRANS ? 1 : (size_t)ldda;
         for (int j = 0; j < n; j++) {
-            const double a = Ai[(size_t)j * ldda];
+            const double a = Ai[(size_t)j * step];
 #pragma unroll
             for (int c = 0; c < NR; c++) acc[c] = fma(-a, sX[j * NR + c], acc[c]);
         }
@@ -387,7 +504,7 @@ __global__ void ir_final_kernel(IrShape sh, unsigned long long *stats, int *iter
             iter[mat] = -itermax - 1;
         }
     }
-    if (st[1] == IR_FAILED) atomicAdd(failed_count, 1);
+    if (st[1] == IR_FAILED || st[1] == IR_FP64) atomicAdd(failed_count, 1);
 }
 
 // Gathers the failed matrices into compact pointer arrays and restarts their
@@ -443,7 +560,7 @@ static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct IrLayout {
     size_t stats, count, asp, as, r, perm, ca, cp, cx, cidx, cinfo, rsc, csc, tc, tc_bytes;
-    size_t ldas_arr, csize, vbw, total;
+    size_t ldas_arr, csize, vbw, ca2, cp2, csize2, total;
     int ldas;
 };
 
@@ -465,8 +582,11 @@ static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900, bool vb = 
     L.cx = o;    o = align256(o + (size_t)batch * sizeof(double *));
     L.cidx = o;  o = align256(o + (size_t)batch * sizeof(int));
     L.cinfo = o; o = align256(o + (size_t)batch * sizeof(int));
-    L.ldas_arr = L.csize = L.vbw = o;
+    L.ca2 = o;   o = align256(o + (size_t)batch * sizeof(double *));   // adjoint fallback lists
+    L.cp2 = o;   o = align256(o + (size_t)batch * sizeof(int *));
+    L.ldas_arr = L.csize = L.csize2 = L.vbw = o;
     if (vb) {
+        L.csize2 = o;   o = align256(o + 2 * (size_t)batch * sizeof(int));
         L.ldas_arr = o; o = align256(o + (size_t)batch * sizeof(int));
         L.csize = o;    o = align256(o + 4 * (size_t)batch * sizeof(int));
         L.vbw = o;      o = align256(o + vb_work_bytes(batch));
@@ -490,26 +610,56 @@ static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900, bool vb = 
     return L;
 }
 
-template <int NR>
+template <int NR, bool TRANS>
 static void launch_residual(const IrShape &sh, double **dA, double **dB, double **dX, double *R,
                             unsigned long long *stats, int par, int batch, cudaStream_t s)
 {
     const size_t smem = (size_t)sh.n * NR * sizeof(double);
     static size_t dyn_max = 0;
-    if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(ir_residual_kernel<NR>);
+    if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(ir_residual_kernel<NR, TRANS>);
     MLU_LAUNCH(mlu::KC_IR_RESIDUAL, s,
-               ir_residual_kernel<NR><<<dim3((sh.n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS, smem, s>>>(
-                   sh, dA, dB, dX, R, stats, par));
+               ir_residual_kernel<NR, TRANS><<<dim3((sh.n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS,
+                                               smem, s>>>(sh, dA, dB, dX, R, stats, par));
 }
 
+template <bool TRANS>
 static void residual(const IrShape &sh, double **dA, double **dB, double **dX, double *R,
                      unsigned long long *stats, int par, int batch, cudaStream_t s)
 {
-    if (sh.nrhs <= 1)      launch_residual<1>(sh, dA, dB, dX, R, stats, par, batch, s);
-    else if (sh.nrhs <= 2) launch_residual<2>(sh, dA, dB, dX, R, stats, par, batch, s);
-    else if (sh.nrhs <= 4) launch_residual<4>(sh, dA, dB, dX, R, stats, par, batch, s);
-    else if (sh.nrhs <= 8) launch_residual<8>(sh, dA, dB, dX, R, stats, par, batch, s);
-    else                   launch_residual<16>(sh, dA, dB, dX, R, stats, par, batch, s);
+    if (sh.nrhs <= 1)      launch_residual<1, TRANS>(sh, dA, dB, dX, R, stats, par, batch, s);
+    else if (sh.nrhs <= 2) launch_residual<2, TRANS>(sh, dA, dB, dX, R, stats, par, batch, s);
+    else if (sh.nrhs <= 4) launch_residual<4, TRANS>(sh, dA, dB, dX, R, stats, par, batch, s);
+    else if (sh.nrhs <= 8) launch_residual<8, TRANS>(sh, dA, dB, dX, R, stats, par, batch, s);
+    else                   launch_residual<16, TRANS>(sh, dA, dB, dX, R, stats, par, batch, s);
+}
+
+// check + correction solve of refinement iteration `it` (-1: the initial solve)
+template <bool TRANS>
+static void correction_solve(const IrShape &sh, float **As_array, int ldas, const int *perm,
+                             double **dX, const double *R, unsigned long long *stats, int *iter,
+                             const int *info, int it, double tol, const double *rsc,
+                             const double *csc, int batch, cudaStream_t s)
+{
+    const int snr = sh.nrhs <= 4 ? 4 : IR_SOLVE_NR;   // right-hand sides per CTA
+    const size_t ssmem = (size_t)snr * sh.n * sizeof(float);
+    const dim3 grid(mlu_ceildiv(sh.nrhs, snr), batch);
+    if (snr == 4)
+        MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4, TRANS><<<grid, 256, ssmem, s>>>(
+            sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, rsc, csc));
+    else
+        MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<IR_SOLVE_NR, TRANS><<<grid, 256, ssmem, s>>>(
+            sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, rsc, csc));
+}
+
+static size_t solve_dyn_max()
+{
+    static size_t v = 0;
+    if (!v)
+        v = min(min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false>),
+                    mlu_allow_dynamic_smem(ir_solve_kernel<4, false>)),
+                min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, true>),
+                    mlu_allow_dynamic_smem(ir_solve_kernel<4, true>)));
+    return v;
 }
 
 }  // namespace mlu
@@ -538,11 +688,7 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
     if (*lwork < L.total) return -15;
     if (n == 0 || nrhs == 0 || batchCount <= 0) return 0;
     // shared-memory limits of the correction solve and the residual kernels
-    static size_t solve_dyn_max = 0;
-    if (!solve_dyn_max)
-        solve_dyn_max = min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR>),
-                            mlu_allow_dynamic_smem(ir_solve_kernel<4>));
-    if ((size_t)IR_SOLVE_NR * n * sizeof(float) > solve_dyn_max ||
+    if ((size_t)IR_SOLVE_NR * n * sizeof(float) > solve_dyn_max() ||
         (size_t)n * IR_NRHS_MAX * sizeof(double) > 200 * 1024)
         return MAGMA_ERR_NOT_SUPPORTED;
 
@@ -582,26 +728,15 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
     int *perm = (int *)(w + L.perm);
     MLU_LAUNCH(mlu::KC_OTHER, s, ir_perm_kernel<<<batchCount, 256, (size_t)n * sizeof(int), s>>>(
         sh, dipiv_array, perm));
-    // right-hand sides per solve CTA: 4 when they fit, else 8
-    const int snr = nrhs <= 4 ? 4 : IR_SOLVE_NR;
-    const size_t ssmem = (size_t)snr * n * sizeof(float);
     auto solve = [&](int it) {
-        const dim3 grid(mlu_ceildiv(nrhs, snr), batchCount);
-        if (snr == 4)
-            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4><<<grid, 256, ssmem, s>>>(
-                sh, As_array, L.ldas, perm, dX_array, R, stats, diter_array, dinfo_array, it,
-                tol, rsc, csc));
-        else
-            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<IR_SOLVE_NR><<<grid, 256, ssmem, s>>>(
-                sh, As_array, L.ldas, perm, dX_array, R, stats, diter_array, dinfo_array, it,
-                tol, rsc, csc));
+        correction_solve<false>(sh, As_array, L.ldas, perm, dX_array, R, stats, diter_array,
+                                dinfo_array, it, tol, rsc, csc, batchCount, s);
     };
-
     solve(-1);
-    residual(sh, dA_array, dB_array, dX_array, R, stats, 0, batchCount, s);
+    residual<false>(sh, dA_array, dB_array, dX_array, R, stats, 0, batchCount, s);
     for (int it = 0; it < itermax; it++) {
         solve(it);
-        residual(sh, dA_array, dB_array, dX_array, R, stats, (it + 1) & 1, batchCount, s);
+        residual<false>(sh, dA_array, dB_array, dX_array, R, stats, (it + 1) & 1, batchCount, s);
     }
     MLU_LAUNCH(mlu::KC_OTHER, s, ir_final_kernel<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(
         sh, stats, diter_array, itermax, tol, batchCount, count));
@@ -633,6 +768,129 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
     if (rc != 0) return rc;
     MLU_LAUNCH(mlu::KC_OTHER, s, ir_scatter_info_kernel<<<mlu_ceildiv(failed, 256), 256, 0, s>>>(
         failed, cidx, cinfo, dinfo_array));
+    MLU_CHECK_LAUNCH();
+    return 0;
+}
+
+// The FP64 part of the adjoint: compacts the matrices the refinement left
+// unsolved (list 1: all, GB restarted from G; list 2: those still needing an
+// FP64 factorisation), factors list 2 in place and solves list 1 with A^T.
+static magma_int_t adjoint_fp64_solves(const IrShape &sh, const IrLayout &L, char *w,
+                                       double **dA_array, magma_int_t **dipiv_array,
+                                       double **dG_array, double **dGB_array,
+                                       magma_int_t *dinfo_array, int batchCount,
+                                       magma_queue_t queue)
+{
+    const bool vb = sh.n_arr != nullptr;
+    const int n = sh.n, nrhs = sh.nrhs;
+    cudaStream_t s = queue->stream;
+    unsigned long long *stats = (unsigned long long *)(w + L.stats);
+    int *count = (int *)(w + L.count);
+    int cnt[2] = {0, 0};
+    cudaMemcpyAsync(&cnt[0], count, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return MAGMA_ERR_UNKNOWN;
+    if (cnt[0] == 0) return 0;
+    double **cA = (double **)(w + L.ca);
+    int **cP = (int **)(w + L.cp);
+    double **cGB = (double **)(w + L.cx);
+    int *csize = vb ? (int *)(w + L.csize) : nullptr;
+    double **cA2 = (double **)(w + L.ca2);
+    int **cP2 = (int **)(w + L.cp2);
+    int *cidx2 = (int *)(w + L.cidx);
+    int *cinfo2 = (int *)(w + L.cinfo);
+    int *csize2 = vb ? (int *)(w + L.csize2) : nullptr;
+    cudaMemsetAsync(count + 1, 0, 2 * sizeof(int), s);
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_compact_adj_kernel<<<batchCount, 256, 0, s>>>(
+        sh, dA_array, dipiv_array, dG_array, dGB_array, stats, batchCount, count + 1, cA, cP, cGB,
+        csize, cA2, cP2, cidx2, csize2));
+    cudaMemcpyAsync(cnt, count + 1, 2 * sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return MAGMA_ERR_UNKNOWN;
+    magma_int_t rc = 0;
+    if (cnt[1] > 0) {
+        if (vb)
+            rc = vb_run<double>(csize2, csize2, nullptr, n, n, 0, cA2, csize2 + batchCount, cP2,
+                                nullptr, nullptr, cinfo2, w + L.vbw, cnt[1], queue, nullptr);
+        else
+            rc = magma_dgetrf_batched(n, n, cA2, sh.lda, cP2, cinfo2, cnt[1], queue);
+        if (rc != 0) return rc;
+        MLU_LAUNCH(mlu::KC_OTHER, s, ir_scatter_info_kernel<<<mlu_ceildiv(cnt[1], 256), 256, 0, s>>>(
+            cnt[1], cidx2, cinfo2, dinfo_array));
+    }
+    if (vb)
+        return vb_getrs_run<double>(true, csize, csize + batchCount, n, nrhs, cA,
+                                    csize + 2 * batchCount, cP, cGB, csize + 3 * batchCount,
+                                    cnt[0], queue);
+    return magma_dgetrs_batched(MagmaTrans, n, nrhs, cA, sh.lda, cP, cGB, sh.ldx, cnt[0], queue);
+}
+
+// Adjoint of a refinement solve: GB = A^{-T} G with the FP32 factors the
+// forward call (precision 900, same workspace, same sizes) left in `work`,
+// refined in FP64 like the forward solve (residual G - A^T GB); then, when
+// dGA is given, GA = -GB X^T.  Matrices whose forward solve fell back
+// (iter_fwd < 0: A holds FP64 factors) and, with `fallback`, matrices whose
+// adjoint refinement does not converge (A is then factored in FP64 in place,
+// info and ipiv overwritten) get an FP64 transposed solve.  `sh` describes A,
+// G (ldb) and GB (ldx).
+static magma_int_t
+ir_run_adjoint(const IrShape &sh, double **dA_array, magma_int_t **dipiv_array, double **dX_array,
+               const int *lddx_arr, int lddx, double **dG_array, double **dGB_array,
+               double **dGA_array, const int *lddga_arr, int lddga, const int *diter_fwd,
+               magma_int_t *dinfo_array, magma_int_t *diter_array, magma_int_t itermax, double tol,
+               magma_int_t fallback, void *work, size_t lwork, magma_int_t batchCount,
+               magma_queue_t queue)
+{
+    const bool vb = sh.n_arr != nullptr;
+    const int n = sh.n, nrhs = sh.nrhs;
+    const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0), 900, vb);
+    if (work == nullptr || lwork < L.total) return MAGMA_ERR_UNKNOWN;   // checked by the callers
+    if (n == 0 || nrhs == 0 || batchCount <= 0) return 0;
+    if ((size_t)IR_SOLVE_NR * n * sizeof(float) > solve_dyn_max() ||
+        (size_t)n * IR_NRHS_MAX * sizeof(double) > 200 * 1024)
+        return MAGMA_ERR_NOT_SUPPORTED;
+    cudaStream_t s = queue->stream;
+    char *w = (char *)work;
+    unsigned long long *stats = (unsigned long long *)(w + L.stats);
+    int *count = (int *)(w + L.count);
+    float **As_array = (float **)(w + L.asp);
+    double *R = (double *)(w + L.r);
+    const int *perm = (const int *)(w + L.perm);
+
+    cudaMemsetAsync(w, 0, L.asp, s);   // stats and counters of this solve; the factors stay
+    const dim3 rows_grid((n + IR_ROWS - 1) / IR_ROWS, batchCount);
+    MLU_LAUNCH(mlu::KC_IR_INIT, s, ir_init_adj_kernel<<<rows_grid, IR_ROWS, 0, s>>>(
+        sh, dA_array, dG_array, dGB_array, R, stats, diter_fwd, diter_array));
+    auto solve = [&](int it) {
+        correction_solve<true>(sh, As_array, L.ldas, perm, dGB_array, R, stats, diter_array,
+                               nullptr, it, tol, nullptr, nullptr, batchCount, s);
+    };
+    solve(-1);
+    residual<true>(sh, dA_array, dG_array, dGB_array, R, stats, 0, batchCount, s);
+    for (int it = 0; it < itermax; it++) {
+        solve(it);
+        residual<true>(sh, dA_array, dG_array, dGB_array, R, stats, (it + 1) & 1, batchCount, s);
+    }
+    MLU_LAUNCH(mlu::KC_OTHER, s, ir_final_kernel<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(
+        sh, stats, diter_array, itermax, tol, batchCount, count));
+    MLU_CHECK_LAUNCH();
+
+    // FP64 transposed solves for matrices the refinement did not solve (without
+    // `fallback`: none, and no synchronisation, so the call can be captured)
+    if (fallback) {
+        const magma_int_t rc = adjoint_fp64_solves(sh, L, w, dA_array, dipiv_array, dG_array,
+                                                   dGB_array, dinfo_array, batchCount, queue);
+        if (rc != 0) return rc;
+    }
+    if (dGA_array) {
+        magma_int_t rc;
+        if (vb)
+            rc = ger_neg_vbatched<double>(sh.n_arr, sh.nrhs_arr, n, dGB_array, sh.ldx_arr,
+                                          dX_array, lddx_arr, dGA_array, lddga_arr, batchCount,
+                                          queue);
+        else
+            rc = magmablas_dger_neg_batched(n, nrhs, dGB_array, sh.ldx, dX_array, lddx, dGA_array,
+                                            lddga, batchCount, queue);
+        if (rc != 0) return rc;
+    }
     MLU_CHECK_LAUNCH();
     return 0;
 }
@@ -743,13 +1001,76 @@ magma_dxgesv_vbatched_work(magma_int_t precision, magma_int_t *n, magma_int_t *n
         magma_xerbla(__func__, -info);
         return info;
     }
-    const IrShape sh = {max_n, max_nrhs, 0, 0, 0, n, nrhs, ldda, lddb, lddx};
-    if (work != nullptr) {
-        size_t need = 0;
-        ir_run(900, sh, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, itermax, tol, 0,
-               nullptr, &need, batchCount, queue);
-        if (*lwork < need) return -18;
+    const size_t need = ir_layout(max_n, max_nrhs, batchCount, 900, true).total;
+    if (work == nullptr) {          // workspace query
+        *lwork = need;
+        return 0;
     }
+    if (*lwork < need) return -18;
+    const IrShape sh = {max_n, max_nrhs, 0, 0, 0, n, nrhs, ldda, lddb, lddx};
     return ir_run(900, sh, dA_array, dipiv_array, dB_array, dX_array, dinfo_array, diter_array,
                   itermax, tol, fallback, work, lwork, batchCount, queue);
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of the refinement solve (no counterpart in the reference).
+
+extern "C" magma_int_t
+magma_dxgesv_adjoint_batched_work(magma_int_t n, magma_int_t nrhs, double **dA_array,
+                                  magma_int_t ldda, magma_int_t **dipiv_array, double **dX_array,
+                                  magma_int_t lddx, double **dG_array, magma_int_t lddg,
+                                  double **dGB_array, magma_int_t lddgb, double **dGA_array,
+                                  magma_int_t lddga, magma_int_t *diter_fwd,
+                                  magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                  magma_int_t itermax, double tol, magma_int_t fallback,
+                                  void *work, size_t lwork, magma_int_t batchCount,
+                                  magma_queue_t queue)
+{
+    magma_int_t info = 0;
+    if (n < 0) info = -1;
+    else if (nrhs < 0 || nrhs > IR_NRHS_MAX) info = -2;
+    else if (ldda < mlu_max(1, n)) info = -4;
+    else if (lddx < mlu_max(1, n)) info = -7;
+    else if (lddg < mlu_max(1, n)) info = -9;
+    else if (lddgb < mlu_max(1, n)) info = -11;
+    else if (dGA_array != nullptr && lddga < mlu_max(1, n)) info = -13;
+    else if (itermax < 0) info = -17;
+    else if (batchCount < 0) info = -22;
+    else if (work == nullptr || lwork < ir_layout(n, nrhs, batchCount, 900, false).total) info = -21;
+    if (info != 0) {
+        magma_xerbla(__func__, -info);
+        return info;
+    }
+    const IrShape sh = {n, nrhs, ldda, lddg, lddgb, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return ir_run_adjoint(sh, dA_array, dipiv_array, dX_array, nullptr, lddx, dG_array, dGB_array,
+                          dGA_array, nullptr, lddga, diter_fwd, dinfo_array, diter_array, itermax,
+                          tol, fallback, work, lwork, batchCount, queue);
+}
+
+extern "C" magma_int_t
+magma_dxgesv_adjoint_vbatched_work(magma_int_t *n, magma_int_t *nrhs, magma_int_t max_n,
+                                   magma_int_t max_nrhs, double **dA_array, magma_int_t *ldda,
+                                   magma_int_t **dipiv_array, double **dX_array, magma_int_t *lddx,
+                                   double **dG_array, magma_int_t *lddg, double **dGB_array,
+                                   magma_int_t *lddgb, double **dGA_array, magma_int_t *lddga,
+                                   magma_int_t *diter_fwd, magma_int_t *dinfo_array,
+                                   magma_int_t *diter_array, magma_int_t itermax, double tol,
+                                   magma_int_t fallback, void *work, size_t lwork,
+                                   magma_int_t batchCount, magma_queue_t queue)
+{
+    magma_int_t info = 0;
+    if (max_n < 0) info = -3;
+    else if (max_nrhs < 0 || max_nrhs > IR_NRHS_MAX) info = -4;
+    else if (itermax < 0) info = -19;
+    else if (batchCount < 0) info = -24;
+    else if (work == nullptr || lwork < ir_layout(max_n, max_nrhs, batchCount, 900, true).total)
+        info = -23;
+    if (info != 0) {
+        magma_xerbla(__func__, -info);
+        return info;
+    }
+    const IrShape sh = {max_n, max_nrhs, 0, 0, 0, n, nrhs, ldda, lddg, lddgb};
+    return ir_run_adjoint(sh, dA_array, dipiv_array, dX_array, lddx, 0, dG_array, dGB_array,
+                          dGA_array, lddga, 0, diter_fwd, dinfo_array, diter_array, itermax, tol,
+                          fallback, work, lwork, batchCount, queue);
 }

@@ -33,18 +33,40 @@ namespace mlu {
 constexpr int PANEL_THREADS = PANEL_REGS_THREADS;
 constexpr int SWAP_THREADS = 128;
 
+// Per-matrix sizes for a variable-size batch (device arrays, or all null for a
+// uniform batch).  The step kernels take this matrix's m, n, ld from them, do
+// nothing when the matrix is already factored past column j0, and narrow the
+// panel to the matrix's last columns.
+struct StepSizes {
+    const int *m_arr, *n_arr, *ld_arr;
+    __device__ __forceinline__ bool get(int mat, int j0, int &m, int &n, int &ld, int &ib) const
+    {
+        if (m_arr) {
+            m = m_arr[mat];
+            n = n_arr[mat];
+            ld = ld_arr[mat];
+        }
+        const int mn = min(m, n);
+        if (j0 >= mn) return false;
+        ib = min(ib, mn - j0);
+        return true;
+    }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(PANEL_THREADS)
 panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
-             int *info_array)
+             int *info_array, StepSizes vs)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int s_ipiv[PANEL_NB];
     const int mat = blockIdx.x, tid = threadIdx.x;
-    T *A0 = dA_array[mat];
-    T *A = A0 + j0 + (size_t)j0 * ldda;
+    if (!vs.get(mat, j0, m, n, ldda, ib)) {
+        if (j0 == 0 && tid == 0) info_array[mat] = 0;    // empty matrix
+        return;
+    }
+    T *A = dA_array[mat] + j0 + (size_t)j0 * ldda;
     const int info_local = panel_factor<T>(m - j0, ib, A, ldda, smem_raw, s_ipiv, j0);
-    (void)A0;
     if (tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
     if (tid == 0) {
         if (j0 == 0) info_array[mat] = info_local;
@@ -58,11 +80,15 @@ panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_ar
 template <typename T, int RPT>
 __global__ void __launch_bounds__(PANEL_THREADS, (sizeof(T) * RPT * PANEL_NB / 4 > 64) ? 1 : 2)
 panel_regs_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
-                  int *info_array)
+                  int *info_array, StepSizes vs)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int s_ipiv[PANEL_NB];
     const int mat = blockIdx.x, tid = threadIdx.x;
+    if (!vs.get(mat, j0, m, n, ldda, ib)) {
+        if (j0 == 0 && tid == 0) info_array[mat] = 0;    // empty matrix
+        return;
+    }
     T *A = dA_array[mat] + j0 + (size_t)j0 * ldda;
     const int info_local = panel_factor_regs<T, RPT>(m - j0, ib, A, ldda, s_ipiv, j0, smem);
     if (tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
@@ -90,12 +116,14 @@ constexpr int SWAP_COLS = 64;
 
 template <typename T>
 __global__ void __launch_bounds__(SWAP_THREADS)
-swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array)
+swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
+                 StepSizes vs)
 {
     __shared__ int s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt;
     __shared__ T s_tmp[2 * PANEL_NB * (SWAP_W + 1)];
     __shared__ T s_rhs[PANEL_NB * SWAP_COLS];
     const int mat = blockIdx.y;
+    if (!vs.get(mat, j0, m, n, ldda, ib)) return;
     T *A = dA_array[mat];
     // column tile: left tiles cover [0, j0), right tiles cover [j0+ib, n)
     const int nleft = (j0 + SWAP_COLS - 1) / SWAP_COLS;
@@ -109,6 +137,7 @@ swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipi
         c0 = j0 + ib + (blockIdx.x - nleft) * SWAP_COLS;
         c1 = min(c0 + SWAP_COLS, n);
         right = true;
+        if (c0 >= n) return;             // past this matrix's columns
     }
     if (threadIdx.x < 32) build_permutation(ipiv_array[mat], j0, ib, s_row, s_src, &s_cnt);
     __syncthreads();
@@ -119,11 +148,13 @@ swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipi
 // A22 -= L21 * U12 on BM x BN tiles, TM x TN accumulators per thread.
 template <typename T, int BM, int BN, int TM, int TN>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
-gemm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int tiles_m)
+gemm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int tiles_m, StepSizes vs)
 {
     __shared__ __align__(16) T sL[PANEL_NB * BM];
     __shared__ __align__(16) T sU[BN * GEMM_LDU];
     const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
+    if (!vs.get(blockIdx.y, j0, m, n, ldda, ib)) return;
+    if (j0 + ib + tm * BM >= m || j0 + ib + tn * BN >= n) return;   // tile past this matrix
     gemm_tile<T, BM, BN, TM, TN>(dA_array[blockIdx.y], ldda, m, n, j0, ib, j0 + ib + tm * BM,
                                  j0 + ib + tn * BN, sL, sU);
 }
@@ -140,9 +171,11 @@ int blocked_panel_width(int m, int n, int j0)
 
 // One step of the blocked factorisation for every matrix: panel at column j0
 // of width ib, interchanges + TRSM, and (when `update`) the trailing update.
+// `vsz`: per-matrix sizes of a variable-size batch (m, n = their maxima).
 template <typename T>
-magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int *info, int batch,
-                                magma_queue_t q, int j0, int ib, bool update)
+magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, int *info, int batch,
+                                  magma_queue_t q, int j0, int ib, bool update,
+                                  StepSizes vsz = {nullptr, nullptr, nullptr})
 {
     cudaStream_t s = q->stream;
     constexpr int BM = 64, BN = 64, TM = 4, TN = 4;
@@ -166,35 +199,49 @@ magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int 
         T **dAb = dA + b0;
         int **ipb = ipiv + b0;
         int *infb = info + b0;
+        StepSizes vs = vsz;
+        if (vs.m_arr) {
+            vs.m_arr += b0;
+            vs.n_arr += b0;
+            vs.ld_arr += b0;
+        }
         // panel (one CTA per matrix), then interchanges + TRSM (one CTA per
         // matrix and 64-column tile)
         if (rpt == 1)
-            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 1><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb));
+            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 1><<<nb, PANEL_THREADS, smem, s>>>(
+                m, n, j0, ib, dAb, ldda, ipb, infb, vs));
         else if (rpt == 2)
-            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 2><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb));
+            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 2><<<nb, PANEL_THREADS, smem, s>>>(
+                m, n, j0, ib, dAb, ldda, ipb, infb, vs));
         else if (rpt == 4)
-            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2)><<<nb, PANEL_THREADS, smem, s>>>(
-                m, n, j0, ib, dAb, ldda, ipb, infb));
+            MLU_LAUNCH(mlu::KC_PANEL, s,
+                       panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2)><<<nb, PANEL_THREADS, smem, s>>>(
+                           m, n, j0, ib, dAb, ldda, ipb, infb, vs));
         else
-            MLU_LAUNCH(mlu::KC_PANEL, s, panel_kernel<T><<<nb, PANEL_THREADS, smem, s>>>(m, n, j0, ib, dAb, ldda, ipb, infb));
+            MLU_LAUNCH(mlu::KC_PANEL, s, panel_kernel<T><<<nb, PANEL_THREADS, smem, s>>>(
+                m, n, j0, ib, dAb, ldda, ipb, infb, vs));
         const int ncl = (j0 + SWAP_COLS - 1) / SWAP_COLS;
         const int ncr = (n - j0 - ib + SWAP_COLS - 1) / SWAP_COLS;
         if (ncl + ncr > 0)
-            MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, swap_trsm_kernel<T><<<dim3(ncl + ncr, nb), SWAP_THREADS, 0, s>>>(m, n, j0, ib, dAb,
-                                                                          ldda, ipb));
+            MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, swap_trsm_kernel<T><<<dim3(ncl + ncr, nb), SWAP_THREADS, 0, s>>>(
+                m, n, j0, ib, dAb, ldda, ipb, vs));
         const int rm = m - j0 - ib, rn = n - j0 - ib;
         if (update && rm > 0 && rn > 0) {
-            bool done = false;
-            if (!done) {
-                const int tiles_m = (rm + BM - 1) / BM, tiles_n = (rn + BN - 1) / BN;
-                MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
-                                                 (BM / TM) * (BN / TN), 0, s>>>(
-                    m, n, j0, ib, dAb, ldda, tiles_m));
-            }
+            const int tiles_m = (rm + BM - 1) / BM, tiles_n = (rn + BN - 1) / BN;
+            MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
+                                                                            (BM / TM) * (BN / TN), 0, s>>>(
+                m, n, j0, ib, dAb, ldda, tiles_m, vs));
         }
     }
     MLU_CHECK_LAUNCH();
     return MAGMA_SUCCESS;
+}
+
+template <typename T>
+magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int *info, int batch,
+                                magma_queue_t q, int j0, int ib, bool update)
+{
+    return blocked_getrf_steps_l<T>(m, n, dA, ldda, ipiv, info, batch, q, j0, ib, update);
 }
 
 template <typename T>
@@ -205,8 +252,8 @@ magma_int_t blocked_getrf(int m, int n, T **dA, int ldda, int **ipiv, int *info,
     const int mn = min(m, n);
     for (int j0 = 0; j0 < mn;) {
         const int ib = blocked_panel_width<T>(m, n, j0);
-        const magma_int_t rc = blocked_getrf_steps<T>(m, n, dA, ldda, ipiv, info, batch, q, j0, ib,
-                                                      true);
+        const magma_int_t rc = blocked_getrf_steps_l<T>(m, n, dA, ldda, ipiv, info, batch, q, j0,
+                                                        ib, true);
         if (rc != 0) return rc;
         j0 += ib;
     }
@@ -216,6 +263,33 @@ magma_int_t blocked_getrf(int m, int n, T **dA, int ldda, int **ipiv, int *info,
 template int blocked_panel_width<float>(int, int, int);
 template magma_int_t blocked_getrf_steps<float>(int, int, float **, int, int **, int *, int,
                                                 magma_queue_t, int, int, bool);
+
+// Variable-size batch through the step kernels (several CTAs per matrix and
+// step, for batches with large matrices): m, n, ld per matrix on the device,
+// max_m / max_n their maxima.  The steps advance by the panel width every
+// matrix still has columns at; a matrix whose columns are done leaves each
+// launch at once.  Same arithmetic as every other path.
+template <typename T>
+magma_int_t blocked_getrf_vbatched(const int *m, const int *n, const int *ld, int max_m,
+                                   int max_n, T **dA, int **ipiv, int *info, int batch,
+                                   magma_queue_t q)
+{
+    if (batch <= 0 || max_m <= 0 || max_n <= 0) return MAGMA_SUCCESS;
+    const int mn = min(max_m, max_n);
+    const StepSizes vs = {m, n, ld};
+    for (int j0 = 0; j0 < mn;) {
+        const int ib = blocked_panel_width<T>(max_m, max_n, j0);
+        const magma_int_t rc = blocked_getrf_steps_l<T>(max_m, max_n, dA, 0, ipiv, info, batch, q,
+                                                        j0, ib, true, vs);
+        if (rc != 0) return rc;
+        j0 += ib;
+    }
+    return MAGMA_SUCCESS;
+}
+template magma_int_t blocked_getrf_vbatched<double>(const int *, const int *, const int *, int, int,
+                                                    double **, int **, int *, int, magma_queue_t);
+template magma_int_t blocked_getrf_vbatched<float>(const int *, const int *, const int *, int, int,
+                                                   float **, int **, int *, int, magma_queue_t);
 
 // ---------------------------------------------------------------------------
 // Blocked solves.  One CTA per (matrix, group of SOLVE_NR right-hand sides);

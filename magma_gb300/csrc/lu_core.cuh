@@ -336,42 +336,9 @@ __device__ __forceinline__ void apply_permutation(T *A, int lda, int c0, int c1,
 }
 
 // U12 = L11^{-1} A12 for the columns [c0, c1) of the ib rows starting at row
-// j0 (L11 unit lower, at (j0, j0)).  One thread per column, rows in registers,
-// t ascending.  All threads call it; it synchronises on entry and exit.
-template <typename T>
-__device__ __forceinline__ void trsm_l11(T *A, int lda, int j0, int ib, int c0, int c1)
-{
-    __shared__ T s_L[PANEL_NB][PANEL_NB + 1];
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    for (int e = tid; e < ib * ib; e += nthr) {
-        const int i = e % ib, t = e / ib;
-        s_L[i][t] = A[j0 + i + (size_t)(j0 + t) * lda];
-    }
-    __syncthreads();
-    for (int cb = c0; cb < c1; cb += nthr) {
-        if (cb + tid < c1) {
-            T *col = A + j0 + (size_t)(cb + tid) * lda;
-            T u[PANEL_NB];
-#pragma unroll
-            for (int i = 0; i < PANEL_NB; i++) u[i] = i < ib ? col[i] : T(0);
-#pragma unroll
-            for (int t = 0; t < PANEL_NB; t++) {
-                if (t >= ib) break;
-#pragma unroll
-                for (int i = t + 1; i < PANEL_NB; i++)
-                    if (i < ib) u[i] = Prec<T>::fma_(-s_L[i][t], u[t], u[i]);
-            }
-#pragma unroll
-            for (int i = 0; i < PANEL_NB; i++) if (i < ib) col[i] = u[i];
-        }
-    }
-    __syncthreads();
-}
-
-// U12 = L11^{-1} A12 as trsm_l11, with the right-hand sides staged in shared
-// memory (sbuf: PANEL_NB x chunk T) instead of registers: one thread per
-// column, t ascending, so the arithmetic is that of trsm_l11 while the
-// kernel stays light on registers.  All threads call it.
+// j0 (L11 unit lower, at (j0, j0)), the right-hand sides staged in shared
+// memory (sbuf: PANEL_NB x chunk T): one thread per column, updates
+// u_i = fma(-l_it, u_t, u_i) for t ascending.  All threads call it.
 template <typename T>
 __device__ __forceinline__ void trsm_l11_smem(T *A, int lda, int j0, int ib, int c0, int c1,
                                               T *sbuf, int chunk)
@@ -409,7 +376,10 @@ __device__ __forceinline__ void trsm_l11_smem(T *A, int lda, int j0, int ib, int
 // One BM x BN tile of A22 -= L21 * U12 with rows from r0 and columns from c0
 // (rows >= m or columns >= n skipped).  L21 columns j0..j0+ib, U12 rows
 // j0..j0+ib.  sL, sU: PANEL_NB x BM and BN x GEMM_LDU T.  Called by exactly
-// (BM/TM)*(BN/TN) threads; synchronises on entry.
+// (BM/TM)*(BN/TN) threads; synchronises on entry.  Every element is updated
+// acc = fma(-l_k, u_k, acc) for k ascending.  The U12 tile is stored
+// transposed (sU[j][k]) so that its store (lanes down a column of A) and the
+// compute loop's reads (4 consecutive k per thread) are free of bank conflicts.
 template <typename T, int BM, int BN, int TM, int TN>
 __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, int ib, int r0, int c0, T *sL,
                           T *sU)
@@ -421,8 +391,6 @@ __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, i
         const int i = e % BM, k = e / BM;
         sL[k * BM + i] = (r0 + i < m) ? A[r0 + i + (size_t)(j0 + k) * lda] : T(0);
     }
-    // U12 transposed (sU[j][k], row stride GEMM_LDU): lanes run down a column
-    // of A for the load and along k for the store, both conflict-free
     for (int e = tid; e < ib * BN; e += NT) {
         const int k = e % ib, j = e / ib;
         sU[j * GEMM_LDU + k] = (c0 + j < n) ? A[j0 + k + (size_t)(c0 + j) * lda] : T(0);

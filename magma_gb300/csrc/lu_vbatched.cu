@@ -40,6 +40,11 @@ constexpr size_t VB_SMEM_CAP = 220 * 1024;
 // 256, 512, 1024, larger).  Every choice applies the same updates to every
 // element in the same order, so the tuning never changes a result.
 constexpr int VB_TUNE_BINS = 8;
+// Batches whose largest matrix is at most this run in the persistent kernel
+// (one CTA per matrix); larger ones in the per-step kernels of the fixed-size
+// path with per-matrix sizes, where every step of a large matrix spreads over
+// many CTAs.
+constexpr int VB_PERSISTENT_MAX = 256;
 enum VbTile { VB_TILE_64x64 = 0, VB_TILE_32x64 = 1, VB_TILE_32x32 = 2, VB_TILE_COUNT = 3 };
 struct VbTune {
     unsigned char nb[VB_TUNE_BINS];     // panel width: 8, 16 or 32
@@ -251,6 +256,15 @@ size_t vb_smem_bytes(int max_m, int max_n, int max_nrhs)
 
 size_t vb_work_bytes(int batch) { return ((size_t)batch * sizeof(int) + 16 + 255) & ~(size_t)255; }
 
+template <typename T>
+magma_int_t blocked_getrf_vbatched(const int *m, const int *n, const int *ld, int max_m,
+                                   int max_n, T **dA, int **ipiv, int *info, int batch,
+                                   magma_queue_t q);
+template <typename T>
+magma_int_t vb_getrs_run(bool trans, const int *n, const int *nrhs, int max_n, int max_nrhs, T **dA,
+                         const int *ldda, int **ipiv, T **dB, const int *lddb, int batch,
+                         magma_queue_t q);
+
 // Tuning tables in use (one per precision), set by magma_?vbatched_tuning_set
 // or the autotuner.  Defaults: the autotuner's choices on GB300.
 static std::mutex g_tune_mu;
@@ -272,6 +286,14 @@ magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int m
 {
     const VbTune tune = tune_override ? *tune_override : current_tune<T>();
     if (batch <= 0) return 0;
+    if (max(max_m, max_n) > VB_PERSISTENT_MAX) {
+        // large matrices: the per-step kernels, several CTAs per matrix
+        magma_int_t rc = blocked_getrf_vbatched<T>(m, n, ldda, max_m, max_n, dA, ipiv, info,
+                                                   batch, q);
+        if (rc == 0 && max_nrhs > 0)
+            rc = vb_getrs_run<T>(false, n, nrhs, max_n, max_nrhs, dA, ldda, ipiv, dB, lddb, batch, q);
+        return rc;
+    }
     static size_t dyn_max = 0;
     if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(vb_lu_kernel<T>);
     const size_t smem = min(vb_smem_bytes<T>(max_m, max_n, max_nrhs), dyn_max);
@@ -327,6 +349,10 @@ magma_int_t vb_getrs_run(bool trans, const int *n, const int *nrhs, int max_n, i
     MLU_CHECK_LAUNCH();
     return 0;
 }
+
+template magma_int_t vb_getrs_run<double>(bool, const int *, const int *, int, int, double **,
+                                          const int *, int **, double **, const int *, int,
+                                          magma_queue_t);
 
 // Synchronous argument check and maxima (the reference's checker + setup,
 // magmablas/vbatched_check.cu:39-58, magmablas/vbatched_aux.cu:27-87).
@@ -571,7 +597,7 @@ __global__ void vb_trial_arrays_kernel(int k, int n, T *A, int *P, T **dA, int *
 }
 
 static const int VB_TUNE_NB[] = {16, 32};
-constexpr int VB_TUNE_MAX_N = 1024;   // bins above this keep their table entry
+constexpr int VB_TUNE_MAX_N = VB_PERSISTENT_MAX;   // larger bins do not use the table
 
 template <typename T>
 static magma_int_t vb_autotune(int max_n, magma_queue_t q, VbTune *out)

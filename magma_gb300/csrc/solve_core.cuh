@@ -175,11 +175,10 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 T acc[SOLVE_NR];
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
-                const T *Ucol = A + (size_t)i * ldda + t0;
                 if (tb == 32) {
                     T uv[32];
 #pragma unroll
-                    for (int t = 0; t < 32; t++) uv[t] = Ucol[t];
+                    for (int t = 0; t < 32; t++) uv[t] = A[(size_t)i * ldda + t0 + t];
 #pragma unroll
                     for (int t = 0; t < 32; t++)
 #pragma unroll
@@ -187,7 +186,7 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                             acc[c] = Prec<T>::fma_(-uv[t], sB[c * n + t0 + t], acc[c]);
                 } else {
                     for (int t = 0; t < tb; t++) {
-                        const T u = Ucol[t];
+                        const T u = A[(size_t)i * ldda + t0 + t];
 #pragma unroll
                         for (int c = 0; c < SOLVE_NR; c++)
                             acc[c] = Prec<T>::fma_(-u, sB[c * n + t0 + t], acc[c]);
@@ -223,11 +222,10 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 T acc[SOLVE_NR];
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
-                const T *Lcol = A + (size_t)i * ldda + t0;
                 if (tb == 32) {
                     T lv[32];
 #pragma unroll
-                    for (int t = 0; t < 32; t++) lv[t] = Lcol[t];
+                    for (int t = 0; t < 32; t++) lv[t] = A[(size_t)i * ldda + t0 + t];
 #pragma unroll
                     for (int t = 31; t >= 0; t--)
 #pragma unroll
@@ -235,7 +233,7 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                             acc[c] = Prec<T>::fma_(-lv[t], sB[c * n + t0 + t], acc[c]);
                 } else {
                     for (int t = tb - 1; t >= 0; t--) {
-                        const T l = Lcol[t];
+                        const T l = A[(size_t)i * ldda + t0 + t];
 #pragma unroll
                         for (int c = 0; c < SOLVE_NR; c++)
                             acc[c] = Prec<T>::fma_(-l, sB[c * n + t0 + t], acc[c]);

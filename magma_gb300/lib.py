@@ -88,6 +88,16 @@ _PROTOS["magma_dxgesv_vbatched_work"] = ([c_int, c_ptr, c_ptr, c_int, c_int, c_p
                                           c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_int,
                                           C.c_double, c_int, c_ptr, C.POINTER(C.c_size_t), c_int,
                                           c_ptr], c_int)
+_PROTOS["magma_dxgesv_adjoint_batched_work"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_ptr, c_int,
+                                                 c_ptr, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr,
+                                                 c_ptr, c_ptr, c_int, C.c_double, c_int, c_ptr,
+                                                 C.c_size_t, c_int, c_ptr], c_int)
+_PROTOS["magma_dxgesv_adjoint_vbatched_work"] = ([c_ptr, c_ptr, c_int, c_int, c_ptr, c_ptr, c_ptr,
+                                                  c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                                                  c_ptr, c_ptr, c_ptr, c_ptr, c_int, C.c_double,
+                                                  c_int, c_ptr, C.c_size_t, c_int, c_ptr], c_int)
+_PROTOS["magmablas_dger_neg_vbatched"] = ([c_ptr, c_ptr, c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
+                                           c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
 _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],

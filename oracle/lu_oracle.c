@@ -308,6 +308,113 @@ void oracle_dsgesv_batched(int n, int nrhs, double *A, int lda, long strideA, co
                                 iter + k);
 }
 
+/* Adjoint of a refinement solve (the GPU's magma_dxgesv_adjoint_*_work):
+ * GB = A^{-T} G refined in FP64 with the FP32 factors of the forward call, in
+ * the GPU's arithmetic order:
+ *   anrm = max_j of the FP32 sum over i ascending of |(float)a_ij| (||A^T||_inf);
+ *   As = (float)A factored by sgetrf (the forward's factors and pivots);
+ *   GB = 0, R = G; solve: GB = GB + (double)sgetrs('T', As, (float)R);
+ *   residual: r_i = g_i, r_i = fma(-a_ji, gb_j, r_i) for j ascending;
+ *   norms and stopping rules of oracle_dsgesv.
+ * iter_fwd < 0 (the forward fell back; A and ipiv hold FP64 factors): GB = G
+ * solved by dgetrs('T') and iter = iter_fwd.  Not converged and `fallback`:
+ * A and ipiv overwritten by dgetrf, GB = G solved by dgetrs('T'), the return
+ * value is dgetrf's info.  Then GA = -GB X^T (acc = fma(gb_ic, x_jc, acc),
+ * c ascending) when GA is not NULL. */
+int oracle_dsgesv_adjoint(int n, int nrhs, double *A, int lda, int *ipiv, const double *X,
+                          int ldx, const double *G, int ldg, double *GB, int ldgb, double *GA,
+                          int ldga, int iter_fwd, int itermax, double tol, int fallback,
+                          int *iter_out)
+{
+    const double eps = 1.1102230246251565e-16;
+    int iter = 0, info = 0, state = 0;
+    if (iter_fwd < 0) {
+        state = 3;
+        iter = iter_fwd;
+    } else if (n > 0 && nrhs > 0) {
+        float *As = (float *)malloc(sizeof(float) * (size_t)n * n + 4);
+        float *Rs = (float *)malloc(sizeof(float) * (size_t)n * nrhs + 4);
+        double *R = (double *)malloc(sizeof(double) * (size_t)n * nrhs + 8);
+        int *ps = (int *)malloc(sizeof(int) * (size_t)n + 4);
+        double anrm = 0.0;
+        for (int j = 0; j < n; j++) {
+            float cs = 0.0f;
+            for (int i = 0; i < n; i++) {
+                float f = (float)A[i + (size_t)j * lda];
+                cs += fabsf(f);
+                As[i + (size_t)j * n] = f;
+            }
+            if ((double)cs > anrm) anrm = (double)cs;
+        }
+        oracle_sgetrf(n, n, As, n, ps);
+        for (int c = 0; c < nrhs; c++)
+            for (int i = 0; i < n; i++) {
+                R[i + (size_t)c * n] = G[i + (size_t)c * ldg];
+                GB[i + (size_t)c * ldgb] = 0.0;
+            }
+        for (int it = -1; state == 0 && it <= itermax; it++) {
+            if (it >= 0) {
+                double rrow = 0.0, xrow = 0.0;
+                int ok = 1;
+                double cte = anrm * eps * sqrt((double)n);
+                for (int c = 0; c < nrhs; c++) {
+                    double rc = 0.0, xc = 0.0;
+                    for (int i = 0; i < n; i++) {
+                        double ra = fabs(R[i + (size_t)c * n]), xa = fabs(GB[i + (size_t)c * ldgb]);
+                        if (ra > rc) rc = ra;
+                        if (xa > xc) xc = xa;
+                    }
+                    if (!(rc <= xc * cte)) ok = 0;
+                }
+                for (int i = 0; i < n; i++) {
+                    double rs = 0.0, xs = 0.0;
+                    for (int c = 0; c < nrhs; c++) {
+                        rs += fabs(R[i + (size_t)c * n]);
+                        xs += fabs(GB[i + (size_t)c * ldgb]);
+                    }
+                    if (rs > rrow) rrow = rs;
+                    if (xs > xrow) xrow = xs;
+                }
+                if (tol > 0.0) ok = rrow <= tol * (anrm * xrow * (double)n * eps);
+                if (ok) { state = 1; iter = it; break; }
+                if (it == itermax) { state = 2; iter = -itermax - 1; break; }
+            }
+            for (size_t e = 0; e < (size_t)n * nrhs; e++) Rs[e] = (float)R[e];
+            oracle_sgetrs(1, n, nrhs, As, n, ps, Rs, n);
+            for (int c = 0; c < nrhs; c++)
+                for (int i = 0; i < n; i++)
+                    GB[i + (size_t)c * ldgb] = GB[i + (size_t)c * ldgb] + (double)Rs[i + (size_t)c * n];
+            for (int c = 0; c < nrhs; c++)
+                for (int i = 0; i < n; i++) {
+                    double acc = G[i + (size_t)c * ldg];
+                    for (int j = 0; j < n; j++)
+                        acc = fma(-A[j + (size_t)i * lda], GB[j + (size_t)c * ldgb], acc);
+                    R[i + (size_t)c * n] = acc;
+                }
+        }
+        free(As); free(Rs); free(R); free(ps);
+    }
+    if (state == 2 && fallback) {
+        info = oracle_dgetrf(n, n, A, lda, ipiv);
+        state = 3;
+    }
+    if (state == 3) {
+        for (int c = 0; c < nrhs; c++)
+            for (int i = 0; i < n; i++) GB[i + (size_t)c * ldgb] = G[i + (size_t)c * ldg];
+        oracle_dgetrs(1, n, nrhs, A, lda, ipiv, GB, ldgb);
+    }
+    if (GA)
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < n; i++) {
+                double acc = 0.0;
+                for (int c = 0; c < nrhs; c++)
+                    acc = fma(GB[i + (size_t)c * ldgb], X[j + (size_t)c * ldx], acc);
+                GA[i + (size_t)j * ldga] = -acc;
+            }
+    *iter_out = iter;
+    return info;
+}
+
 /* Adjoint of x = A^{-1} b with the forward LU kept: G <- A^{-T} G (getrs with
  * TRANS='T'), then GA(i,j) = -(sum_c G(i,c) X(j,c)) accumulated as
  * acc = fma(G(i,c), X(j,c), acc) for c ascending from acc = 0. */

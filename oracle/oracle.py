@@ -229,6 +229,30 @@ def dsgesv_vbatched(As, Bs, itermax=30, tol=0.0, fallback=True):
     return Xs, pivs, info, iters
 
 
+def dsgesv_adjoint(A, ipiv, X, G, iter_fwd, itermax=30, tol=0.0, fallback=True):
+    """Adjoint of one refinement solve (oracle_dsgesv_adjoint).  A: (n, ld) storage as the
+    forward call left it (overwritten on fallback), ipiv: (n,) int32, X and G: (nrhs, ld)
+    storage.  Returns (GB, GA, info, iter) with GB like G and GA (n, n) storage."""
+    lib = load()
+    n, lda = A.shape
+    nrhs, ldx = X.shape
+    ldg = G.shape[1]
+    assert A.flags.c_contiguous and A.dtype == np.float64
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    GB = np.zeros_like(G)
+    GA = np.zeros((n, n), dtype=np.float64)
+    it = np.zeros(1, dtype=np.int32)
+    fn = lib.oracle_dsgesv_adjoint
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                   C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                   C.c_int, C.c_double, C.c_int, C.c_void_p]
+    info = fn(n, nrhs, _p(A), lda, _p(ipiv), _p(np.ascontiguousarray(X)), ldx,
+              _p(np.ascontiguousarray(G)), ldg, _p(GB), ldg, _p(GA), n, int(iter_fwd), itermax,
+              float(tol), 1 if fallback else 0, _p(it))
+    return GB, GA, int(info), int(it[0]), ipiv
+
+
 def gesv_adjoint_batched(LU, ipiv, X, G, nthreads=None):
     """G <- A^{-T} G and returns GA = -G X^T (storage layout), the oracle's
     restatement of the adjoint.  LU (batch, n, ld), X and G (batch, nrhs, ld)."""

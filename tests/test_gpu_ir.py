@@ -155,11 +155,13 @@ def test_dxgesv_fp32_equals_dsgesv(cuda):
     _assert_same(gpu, ref, 100)
 
 
-def _vb_case(seed, count, nmax, rmax, kappa_hi=1e6):
+def _vb_case(seed, count, nmax, rmax, kappa_hi=1e6, kappa_fixed=None):
     rng = np.random.default_rng(seed)
     ns = [int(x) for x in rng.integers(1, nmax + 1, count)]
     rs = [int(x) for x in rng.integers(1, rmax + 1, count)]
     kap = 10.0 ** rng.uniform(0, np.log10(kappa_hi), count)
+    if kappa_fixed is not None:
+        kap[:] = kappa_fixed
     As, Bs = [], []
     for k, (n, r) in enumerate(zip(ns, rs)):
         A = _svd(1, n, [float(kap[k])], seed=seed * 1000 + k)[0]
@@ -174,12 +176,12 @@ def test_dxgesv_vbatched_matches_oracle(cuda, tol):
     iteration counts bit-identical to the oracle matrix by matrix, including matrices with
     kappa 1e9 that fall back to the FP64 re-solve."""
     ns, rs, As, Bs = _vb_case(3, 40, 200, 16)
-    extra = _vb_case(4, 3, 90, 4, kappa_hi=1e10)          # some will not converge
+    extra = _vb_case(4, 3, 90, 4, kappa_fixed=1e10)       # these do not converge in FP32
     ns, rs, As, Bs = ns + extra[0], rs + extra[1], As + extra[2], Bs + extra[3]
     ns.append(1); rs.append(1); As.append(np.array([[3.0]])); Bs.append(np.array([[1.5]]))
     A = mg.VBatch([a.shape for a in As], ns, torch.float64, cuda).load(As)
     B = mg.VBatch([b.shape for b in Bs], ns, torch.float64, cuda).load(Bs)
-    X, ipiv, offs, info, iters = mg.dxgesv_vbatched(A, B, tol=tol)
+    X, ipiv, offs, info, iters, _ = mg.dxgesv_vbatched(A, B, tol=tol)
     torch.cuda.synchronize()
     rA = [a.copy() for a in As]
     rX, rp, rinfo, riters = oracle.dsgesv_vbatched(rA, Bs, tol=tol)
@@ -192,3 +194,61 @@ def test_dxgesv_vbatched_matches_oracle(cuda, tol):
         assert np.array_equal(X.view(k).cpu().numpy(), rX[k], equal_nan=True), k
         assert np.array_equal(A.view(k).cpu().numpy(), rA[k], equal_nan=True), k
     assert (it < 0).any() and (it >= 0).any()
+
+
+def test_dsgesv_adjoint_matches_oracle(cuda):
+    """Adjoint of the refinement solve: GB = A^{-T} G refined with the forward's FP32
+    factors, GA = -GB X^T; bit-identical to the oracle, including matrices whose forward
+    solve fell back to FP64 (kappa 1e10) and use their FP64 factors."""
+    n, nrhs, b = 64, 4, 8
+    kappas = [1e2, 1e4, 1e6, 1e10, 1e3, 1e5, 1e10, 1e1]
+    A = _svd(b, n, kappas, seed=77)
+    Bm = np.random.default_rng(77).uniform(-1, 1, (b, n, nrhs))
+    dS = torch.from_numpy(to_storage(A)).to(cuda)
+    dB = torch.from_numpy(to_storage(Bm)).to(cuda)
+    work = torch.empty((mg.dsgesv_workspace_bytes(n, nrhs, b),), dtype=torch.uint8, device=cuda)
+    X, ipiv, info, iters = mg.dsgesv_batched(dS, dB, work=work)
+    torch.cuda.synchronize()
+    S_fwd, P_fwd, X_h, it_h = dS.cpu().numpy().copy(), ipiv.cpu().numpy(), X.cpu().numpy(), \
+        iters.cpu().numpy()
+    assert (it_h < 0).sum() == 2
+    G = torch.from_numpy(np.random.default_rng(78).standard_normal((b, nrhs, n))).to(cuda)
+    GB, GA, it2 = mg.dsgesv_adjoint_batched(dS, ipiv, X, G, iters, work, info)
+    torch.cuda.synchronize()
+    G_h = G.cpu().numpy()
+    for k in range(b):
+        rGB, rGA, rinfo, rit, _ = oracle.dsgesv_adjoint(S_fwd[k].copy(), P_fwd[k], X_h[k], G_h[k],
+                                                        it_h[k])
+        assert int(it2[k]) == rit, k
+        assert np.array_equal(GB[k].cpu().numpy(), rGB), k
+        assert np.array_equal(GA[k].cpu().numpy(), rGA), k
+    # against an FP64 reference gradient
+    Ad = torch.from_numpy(A)
+    gb_ref = torch.linalg.solve(Ad.transpose(1, 2), torch.from_numpy(G_h).transpose(1, 2))
+    err = (GB.cpu().transpose(1, 2) - gb_ref).abs().amax() / gb_ref.abs().amax()
+    assert float(err) < 1e-6
+
+
+def test_dxgesv_adjoint_vbatched_matches_oracle(cuda):
+    ns, rs, As, Bs = _vb_case(9, 30, 160, 8, kappa_hi=1e5)
+    extra = _vb_case(10, 2, 60, 3, kappa_fixed=1e12)     # forward falls back to FP64
+    ns, rs, As, Bs = ns + extra[0], rs + extra[1], As + extra[2], Bs + extra[3]
+    A = mg.VBatch([a.shape for a in As], ns, torch.float64, cuda).load(As)
+    B = mg.VBatch([b.shape for b in Bs], ns, torch.float64, cuda).load(Bs)
+    X, ipiv, offs, info, iters, work = mg.dxgesv_vbatched(A, B)
+    torch.cuda.synchronize()
+    A_fwd = [A.view(k).cpu().numpy().copy() for k in range(len(ns))]
+    P = ipiv.cpu().numpy()
+    it_h = iters.cpu().numpy()
+    rng = np.random.default_rng(11)
+    Gs = [rng.standard_normal(b.shape) for b in Bs]
+    G = mg.VBatch([g.shape for g in Gs], ns, torch.float64, cuda).load(Gs)
+    GB, GA, it2 = mg.dxgesv_adjoint_vbatched(A, ipiv, offs, X, G, iters, info, work)
+    torch.cuda.synchronize()
+    it2 = it2.cpu().numpy()
+    for k, n in enumerate(ns):
+        rGB, rGA, rinfo, rit, _ = oracle.dsgesv_adjoint(A_fwd[k].copy(), P[offs[k]:offs[k] + n],
+                                                        X.view(k).cpu().numpy(), Gs[k], it_h[k])
+        assert it2[k] == rit, k
+        assert np.array_equal(GB.view(k).cpu().numpy(), rGB), k
+        assert np.array_equal(GA.view(k).cpu().numpy(), rGA), k

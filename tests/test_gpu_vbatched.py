@@ -190,7 +190,7 @@ def test_every_tuning_choice_is_bit_exact(cuda, dtype):
     """Each (panel width, update tile) the tuner can choose, forced on every size bin, gives
     the oracle's factors, pivots and solutions bit for bit."""
     rng = np.random.default_rng(21)
-    ns = [int(n) for n in rng.integers(1, 300, 24)] + [16, 17, 32, 33, 64, 65, 128, 129, 257]
+    ns = [int(n) for n in rng.integers(1, 257, 24)] + [16, 17, 32, 33, 64, 65, 128, 129, 256]
     nrhss = [int(r) for r in rng.integers(1, 17, len(ns))]
     npdt = np.float64 if dtype == torch.float64 else np.float32
     As, Bs = _make(rng, ns, nrhss, ld_pad=1, dtype=npdt)
@@ -234,3 +234,35 @@ def test_autotune_installs_a_valid_table(cuda):
     finally:
         mg.set_vbatched_tuning([saved[b]["nb"] for b in mg.batched.TUNE_BINS],
                                [saved[b]["tile"] for b in mg.batched.TUNE_BINS], torch.float64)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_getrf_vbatched_large_blocked_path(cuda, dtype):
+    """Batches with a matrix above 256 run the per-step kernels with per-matrix sizes:
+    rectangular and square shapes from 1 to 1100, bit-exact with the oracle."""
+    rng = np.random.default_rng(31)
+    shapes = [(700, 300), (300, 700), (513, 513), (1, 900), (900, 1), (64, 64), (1100, 1000),
+              (257, 256), (33, 40), (0, 5), (600, 600)]
+    npdt = np.float64 if dtype == torch.float64 else np.float32
+    ms = [m for m, _ in shapes]
+    ns = [n for _, n in shapes]
+    mats = [rng.uniform(-1, 1, (n, m + 3)).astype(npdt) for m, n in shapes]
+    A = VBatch([a.shape for a in mats], ms, dtype, cuda).load(mats)
+    mn = [max(min(m, n), 1) for m, n in shapes]
+    ipiv = torch.zeros((sum(mn),), dtype=torch.int32, device=cuda)
+    offs = np.concatenate([[0], np.cumsum(mn)[:-1]])
+    dP = ipiv.data_ptr() + torch.tensor(offs, dtype=torch.int64, device=cuda) * 4
+    info = torch.full((len(shapes),), -7, dtype=torch.int32, device=cuda)
+    fn = L.load().magma_dgetrf_vbatched if dtype == torch.float64 else L.load().magma_sgetrf_vbatched
+    rc = fn(_vp(A.rows), _vp(A.ncols), _vp(A.ptrs), _vp(A.ld), _vp(dP), _vp(info), len(shapes),
+            Queue.current(cuda).handle)
+    torch.cuda.synchronize()
+    assert rc == 0
+    P = ipiv.cpu().numpy()
+    inf = info.cpu().numpy()
+    for k, (m, n) in enumerate(shapes):
+        ref = mats[k].copy()
+        rp, rinfo = (oracle.dgetrf if dtype == torch.float64 else oracle.sgetrf)(ref, m)
+        assert inf[k] == rinfo, k
+        assert np.array_equal(A.view(k).cpu().numpy(), ref, equal_nan=True), k
+        assert np.array_equal(P[offs[k]:offs[k] + min(m, n)], rp[:min(m, n)]), k
