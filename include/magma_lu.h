@@ -504,6 +504,60 @@ magma_int_t magmablas_dger_neg_vbatched(magma_int_t *n, magma_int_t *nrhs, magma
                                         magma_int_t *lddx, double **dGA_array, magma_int_t *lddga,
                                         magma_int_t batchCount, magma_queue_t queue);
 
+/* Inverse from the LU factors, out of place (include/magma_zbatched.h:872,
+ * src/zgetri_outofplace_batched.cpp:82): invA = inv(A) = inv(U) inv(L) P^T
+ * for factors and pivots from magma_?getrf_batched.  dA_array is read only;
+ * info_array is not written (as in the reference).  Never synchronises.
+ * Errors: -1 n, -3 ldda, -6 lddia, -8 batchCount; MAGMA_ERR_NOT_SUPPORTED when
+ * 8 columns of order n do not fit in shared memory. */
+magma_int_t magma_dgetri_outofplace_batched(magma_int_t n, double **dA_array, magma_int_t ldda,
+                                            magma_int_t **dipiv_array, double **dinvA_array,
+                                            magma_int_t lddia, magma_int_t *info_array,
+                                            magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetri_outofplace_batched(magma_int_t n, float **dA_array, magma_int_t ldda,
+                                            magma_int_t **dipiv_array, float **dinvA_array,
+                                            magma_int_t lddia, magma_int_t *info_array,
+                                            magma_int_t batchCount, magma_queue_t queue);
+
+/* Strided batches (no counterpart for getrf/getrs/gesv in the reference,
+ * which offers the form for banded LU, magma_zgbtrf_batched_strided,
+ * include/magma_zbatched.h:613): matrix k at dA + k*strideA, its pivots at
+ * dipiv + k*strideP, its right-hand sides at dB + k*strideB (strides in
+ * elements).  The pointer arrays are built on the device in the queue's
+ * scratch (allocated on first use, then reused), then the pointer-array
+ * routine runs: identical results.  Errors: those of the pointer-array
+ * routine, or the position of a stride that is too small. */
+magma_int_t magma_dgetrf_batched_strided(magma_int_t m, magma_int_t n, double *dA,
+                                         magma_int_t ldda, magma_int_t strideA,
+                                         magma_int_t *dipiv, magma_int_t strideP,
+                                         magma_int_t *info_array, magma_int_t batchCount,
+                                         magma_queue_t queue);
+magma_int_t magma_sgetrf_batched_strided(magma_int_t m, magma_int_t n, float *dA,
+                                         magma_int_t ldda, magma_int_t strideA,
+                                         magma_int_t *dipiv, magma_int_t strideP,
+                                         magma_int_t *info_array, magma_int_t batchCount,
+                                         magma_queue_t queue);
+magma_int_t magma_dgetrs_batched_strided(magma_trans_t trans, magma_int_t n, magma_int_t nrhs,
+                                         double *dA, magma_int_t ldda, magma_int_t strideA,
+                                         magma_int_t *dipiv, magma_int_t strideP, double *dB,
+                                         magma_int_t lddb, magma_int_t strideB,
+                                         magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetrs_batched_strided(magma_trans_t trans, magma_int_t n, magma_int_t nrhs,
+                                         float *dA, magma_int_t ldda, magma_int_t strideA,
+                                         magma_int_t *dipiv, magma_int_t strideP, float *dB,
+                                         magma_int_t lddb, magma_int_t strideB,
+                                         magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_dgesv_batched_strided(magma_int_t n, magma_int_t nrhs, double *dA,
+                                        magma_int_t ldda, magma_int_t strideA, magma_int_t *dipiv,
+                                        magma_int_t strideP, double *dB, magma_int_t lddb,
+                                        magma_int_t strideB, magma_int_t *dinfo_array,
+                                        magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgesv_batched_strided(magma_int_t n, magma_int_t nrhs, float *dA,
+                                        magma_int_t ldda, magma_int_t strideA, magma_int_t *dipiv,
+                                        magma_int_t strideP, float *dB, magma_int_t lddb,
+                                        magma_int_t strideB, magma_int_t *dinfo_array,
+                                        magma_int_t batchCount, magma_queue_t queue);
+
 /* ------------------------------------------------------------------------
  * Tuning of the variable-size kernel.  No counterpart in the reference, whose
  * batched routines read fixed crossover tables

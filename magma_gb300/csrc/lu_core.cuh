@@ -317,14 +317,25 @@ template <typename T>
 __device__ __forceinline__ void apply_permutation(T *A, int lda, int c0, int c1, const int *s_row, const int *s_src,
                                   int cnt, T *s_tmp)
 {
-    // rows run fastest across threads, so runs of adjacent rows coalesce
+    // rows run fastest across threads, so runs of adjacent rows coalesce;
+    // eight loads per thread in flight before their stores
     const int tid = threadIdx.x, nthr = blockDim.x;
     if (cnt == 0) return;
     for (int cb = c0; cb < c1; cb += SWAP_W) {
         const int w = min(SWAP_W, c1 - cb);
-        for (int e = tid; e < cnt * w; e += nthr) {
-            const int pr = e % cnt, c = e / cnt;
-            s_tmp[pr * (SWAP_W + 1) + c] = A[s_src[pr] + (size_t)(cb + c) * lda];
+        const int total = cnt * w;
+        for (int e0 = tid; e0 < total; e0 += 8 * nthr) {
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int e = e0 + u * nthr;
+                if (e < total) v[u] = A[s_src[e % cnt] + (size_t)(cb + e / cnt) * lda];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int e = e0 + u * nthr;
+                if (e < total) s_tmp[(e % cnt) * (SWAP_W + 1) + e / cnt] = v[u];
+            }
         }
         __syncthreads();
         for (int e = tid; e < cnt * w; e += nthr) {
@@ -352,9 +363,19 @@ __device__ __forceinline__ void trsm_l11_smem(T *A, int lda, int j0, int ib, int
     for (int cb = c0; cb < c1; cb += chunk) {
         const int w = min(chunk, c1 - cb);
         __syncthreads();
-        for (int e = tid; e < ib * w; e += nthr) {
-            const int i = e % ib, c = e / ib;           // coalesced down each column
-            sbuf[i * chunk + c] = A[j0 + i + (size_t)(cb + c) * lda];
+        const int total = ib * w;
+        for (int e0 = tid; e0 < total; e0 += 8 * nthr) {   // coalesced down each column
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int e = e0 + u * nthr;
+                if (e < total) v[u] = A[j0 + e % ib + (size_t)(cb + e / ib) * lda];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int e = e0 + u * nthr;
+                if (e < total) sbuf[(e % ib) * chunk + e / ib] = v[u];
+            }
         }
         __syncthreads();
         for (int c = tid; c < w; c += nthr) {
@@ -385,15 +406,26 @@ __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, i
                           T *sU)
 {
     constexpr int NT = (BM / TM) * (BN / TN);
+    constexpr int LU_LOADS = PANEL_NB * (BM > BN ? BM : BN) / NT;   // per thread, at most
     const int tid = threadIdx.x;
     __syncthreads();
-    for (int e = tid; e < ib * BM; e += NT) {
-        const int i = e % BM, k = e / BM;
-        sL[k * BM + i] = (r0 + i < m) ? A[r0 + i + (size_t)(j0 + k) * lda] : T(0);
-    }
-    for (int e = tid; e < ib * BN; e += NT) {
-        const int k = e % ib, j = e / ib;
-        sU[j * GEMM_LDU + k] = (c0 + j < n) ? A[j0 + k + (size_t)(c0 + j) * lda] : T(0);
+    {
+        // all of this thread's L21 and U12 loads in flight before the stores
+        T vl[LU_LOADS], vu[LU_LOADS];
+#pragma unroll
+        for (int u = 0; u < LU_LOADS; u++) {
+            const int e = tid + u * NT;
+            const int i = e % BM, kl = e / BM;
+            vl[u] = (kl < ib && r0 + i < m) ? A[r0 + i + (size_t)(j0 + kl) * lda] : T(0);
+            const int ku = e % ib, j = e / ib;
+            vu[u] = (e < ib * BN && c0 + j < n) ? A[j0 + ku + (size_t)(c0 + j) * lda] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < LU_LOADS; u++) {
+            const int e = tid + u * NT;
+            if (e < ib * BM) sL[(e / BM) * BM + e % BM] = vl[u];
+            if (e < ib * BN) sU[(e / ib) * GEMM_LDU + e % ib] = vu[u];
+        }
     }
     const int tr = tid % (BM / TM), tc = tid / (BM / TM);
     T acc[TM][TN];

@@ -98,6 +98,16 @@ _PROTOS["magma_dxgesv_adjoint_vbatched_work"] = ([c_ptr, c_ptr, c_int, c_int, c_
                                                   c_int, c_ptr, C.c_size_t, c_int, c_ptr], c_int)
 _PROTOS["magmablas_dger_neg_vbatched"] = ([c_ptr, c_ptr, c_int, c_ptr, c_ptr, c_ptr, c_ptr, c_ptr,
                                            c_ptr, c_int, c_ptr], c_int)
+for _p in "ds":
+    _PROTOS[f"magma_{_p}getri_outofplace_batched"] = ([c_int, c_ptr, c_int, c_ptr, c_ptr, c_int,
+                                                      c_ptr, c_int, c_ptr], c_int)
+for _p in "ds":
+    _PROTOS[f"magma_{_p}getrf_batched_strided"] = ([c_int, c_int, c_ptr, c_int, c_int, c_ptr, c_int,
+                                                   c_ptr, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}getrs_batched_strided"] = ([c_int, c_int, c_int, c_ptr, c_int, c_int, c_ptr,
+                                                   c_int, c_ptr, c_int, c_int, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}gesv_batched_strided"] = ([c_int, c_int, c_ptr, c_int, c_int, c_ptr, c_int,
+                                                  c_ptr, c_int, c_int, c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
 _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],

@@ -215,6 +215,24 @@ def dsgesv_batched(A, B, itermax=30, tol=0.0, fallback=True, nthreads=None):
     return X, ipiv, info, iters
 
 
+def getri(LU, ipiv):
+    """Inverse from the LU factors, the GPU's order: Y = solve(L, U, I) column by column
+    (getrs arithmetic, no interchanges), then column j of Y is column perm[j] of inv(A), perm
+    the interchanges applied to 0..n-1.  LU: (n, ld) storage; returns (n, n) storage."""
+    n = LU.shape[0]
+    E = np.zeros((n, max(n, 1)), dtype=LU.dtype)
+    E[np.arange(n), np.arange(n)] = 1
+    ident = np.arange(1, n + 1, dtype=np.int32)
+    (dgetrs if LU.dtype == np.float64 else sgetrs)(LU, ident, E)
+    perm = np.arange(n)
+    for k in range(n):
+        p = int(ipiv[k]) - 1
+        perm[k], perm[p] = perm[p], perm[k]
+    Inv = np.empty((n, n), dtype=LU.dtype)
+    Inv[perm] = E[:, :n]
+    return Inv
+
+
 def dsgesv_vbatched(As, Bs, itermax=30, tol=0.0, fallback=True):
     """Variable-size refinement: oracle_dsgesv per matrix.  As[k]: (n_k, ld_k) storage,
     Bs[k]: (nrhs_k, ldb_k).  Returns (Xs, ipivs, info, iters)."""
