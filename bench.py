@@ -1098,12 +1098,37 @@ def run_reference(args, wl):
 # GPU leg
 
 
+def gpu_local_cpus(index):
+    """Host CPUs local to GPU `index` (its PCI device's local_cpulist), or None.  The bench
+    runs on them so that the pinned host buffers of the end-to-end leg sit on the GPU's
+    memory node."""
+    try:
+        out = subprocess.run(["nvidia-smi", f"--id={index}", "--query-gpu=pci.bus_id",
+                              "--format=csv,noheader"], capture_output=True, text=True,
+                             timeout=20).stdout.strip().lower()
+        dom, rest = out.split(":", 1)
+        path = Path(f"/sys/bus/pci/devices/{int(dom, 16):04x}:{rest}/local_cpulist")
+        cpus = set()
+        for part in path.read_text().strip().split(","):
+            lo, _, hi = part.partition("-")
+            cpus.update(range(int(lo), int(hi or lo) + 1))
+        return sorted(cpus) or None
+    except Exception:
+        return None
+
+
 def run_ours(args, wl):
     import torch
     from magma_gb300 import lib as L
     from magma_gb300.batched import Queue
 
     world, rank, local, pg = dist_setup()
+    cpus = gpu_local_cpus(local)
+    if cpus:
+        try:
+            os.sched_setaffinity(0, cpus)
+        except Exception:
+            cpus = None
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     lib = L.load()
@@ -1189,7 +1214,8 @@ def run_ours(args, wl):
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": world * wl.batch / (e2e_ms * 1e-3), "unit": "solves/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                "host_cpus": f"{len(cpus)} GPU-local cores" if cpus else "unpinned"},
         "gpu_launches": launches,
         "clocks": clk,
         "accuracy": {"max_scaled_residual": max_res, "solves_within_30": n_ok, "of": wl.batch,

@@ -262,8 +262,10 @@ __device__ __forceinline__ bool ir_converged(const unsigned long long *st, int p
 
 // check (when it >= 0) + correction solve X += float-solve(R) with the FP32
 // factors.  One CTA per (matrix, group of NR right-hand sides).
+// Four CTAs per SM (64 registers a thread): the solves are latency-bound, so a
+// whole batch of 512 matrices resident at once beats more registers per thread.
 template <int NR, bool TRANS>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double **dX_array,
                 const double *R, unsigned long long *stats, int *iter, const int *info, int it,
                 double tol, const double *rowscale, const double *colscale)
