@@ -60,6 +60,11 @@ typedef enum {
     MagmaConjTrans = 113
 } magma_trans_t;                      /* include/magma_types.h:613-618 */
 
+typedef enum {
+    MagmaFalse = 0,
+    MagmaTrue  = 1
+} magma_bool_t;                       /* include/magma_types.h:600-603 */
+
 /* ------------------------------------------------------------------------ */
 /* Runtime subset -- include/magma_auxiliary.h:24-25, 82-105, 258-330, 357 */
 
@@ -557,6 +562,61 @@ magma_int_t magma_sgesv_batched_strided(magma_int_t n, magma_int_t nrhs, float *
                                         magma_int_t strideP, float *dB, magma_int_t lddb,
                                         magma_int_t strideB, magma_int_t *dinfo_array,
                                         magma_int_t batchCount, magma_queue_t queue);
+
+/* LU without pivoting (include/magma_zbatched.h:977-999,
+ * src/zgetrf_nopiv_batched.cpp): the diagonal entry is the pivot.  info = the
+ * first zero diagonal (1-based); its column is left unscaled.  getrs_nopiv's
+ * info_array is unused, as in the reference.  No allocation or
+ * synchronisation. */
+magma_int_t magma_dgetrf_nopiv_batched(magma_int_t m, magma_int_t n, double **dA_array,
+                                       magma_int_t ldda, magma_int_t *info_array,
+                                       magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetrf_nopiv_batched(magma_int_t m, magma_int_t n, float **dA_array,
+                                       magma_int_t ldda, magma_int_t *info_array,
+                                       magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_dgetrs_nopiv_batched(magma_trans_t trans, magma_int_t n, magma_int_t nrhs,
+                                       double **dA_array, magma_int_t ldda, double **dB_array,
+                                       magma_int_t lddb, magma_int_t *info_array,
+                                       magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sgetrs_nopiv_batched(magma_trans_t trans, magma_int_t n, magma_int_t nrhs,
+                                       float **dA_array, magma_int_t ldda, float **dB_array,
+                                       magma_int_t lddb, magma_int_t *info_array,
+                                       magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_dgesv_nopiv_batched(magma_int_t n, magma_int_t nrhs, double **dA_array,
+                                      magma_int_t ldda, double **dB_array, magma_int_t lddb,
+                                      magma_int_t *info_array, magma_int_t batchCount,
+                                      magma_queue_t queue);
+magma_int_t magma_sgesv_nopiv_batched(magma_int_t n, magma_int_t nrhs, float **dA_array,
+                                      magma_int_t ldda, float **dB_array, magma_int_t lddb,
+                                      magma_int_t *info_array, magma_int_t batchCount,
+                                      magma_queue_t queue);
+
+/* Random butterfly transformation and the solve built on it
+ * (include/magma_zbatched.h:1001-1045, src/zgesv_rbt_batched.cpp,
+ * src/zgerbt_batched.cpp).  Depth-2 recursive butterflies U, V (outer order n,
+ * inner orders ceil(n/2) and n - ceil(n/2)) with random diagonals: U and V
+ * are host arrays of 2n entries, du and dv their device copies.
+ * magma_dgerbt_batched: A <- U^T A V and B <- U^T B for every matrix; with
+ * gen == MagmaTrue it first fills U and V (exp(r/10), r uniform in [-1/2,1/2),
+ * one process-wide stream); copies them to the device and synchronises.
+ * magmablas_dprbt_batched: A <- U^T A V; _mtv: B <- U^T B; _mv: B <- V B.
+ * magma_dgesv_rbt_batched: gerbt, LU without pivoting, solve, x = V y; the
+ * matrix is overwritten by the factors of U^T A V.  No iterative refinement
+ * (as in the reference). */
+magma_int_t magma_dgerbt_batched(magma_bool_t gen, magma_int_t n, magma_int_t nrhs,
+                                 double **dA_array, magma_int_t ldda, double **dB_array,
+                                 magma_int_t lddb, double *U, double *V, magma_int_t *info,
+                                 magma_int_t batchCount, magma_queue_t queue);
+void magmablas_dprbt_batched(magma_int_t n, double **dA_array, magma_int_t ldda, double *du,
+                             double *dv, magma_int_t batchCount, magma_queue_t queue);
+void magmablas_dprbt_mtv_batched(magma_int_t n, magma_int_t nrhs, double *du, double **db_array,
+                                 magma_int_t lddb, magma_int_t batchCount, magma_queue_t queue);
+void magmablas_dprbt_mv_batched(magma_int_t n, magma_int_t nrhs, double *dv, double **db_array,
+                                magma_int_t lddb, magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_dgesv_rbt_batched(magma_int_t n, magma_int_t nrhs, double **dA_array,
+                                    magma_int_t ldda, double **dB_array, magma_int_t lddb,
+                                    magma_int_t *dinfo_array, magma_int_t batchCount,
+                                    magma_queue_t queue);
 
 /* ------------------------------------------------------------------------
  * Tuning of the variable-size kernel.  No counterpart in the reference, whose

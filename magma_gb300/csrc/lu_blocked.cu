@@ -53,7 +53,7 @@ struct StepSizes {
     }
 };
 
-template <typename T>
+template <typename T, bool NOPIV = false>
 __global__ void __launch_bounds__(PANEL_THREADS)
 panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
              int *info_array, StepSizes vs)
@@ -66,8 +66,8 @@ panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_ar
         return;
     }
     T *A = dA_array[mat] + j0 + (size_t)j0 * ldda;
-    const int info_local = panel_factor<T>(m - j0, ib, A, ldda, smem_raw, s_ipiv, j0);
-    if (tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
+    const int info_local = panel_factor<T, NOPIV>(m - j0, ib, A, ldda, smem_raw, s_ipiv, j0);
+    if (ipiv_array && tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
     if (tid == 0) {
         if (j0 == 0) info_array[mat] = info_local;
         else if (info_local != 0 && info_array[mat] == 0) info_array[mat] = info_local;
@@ -77,7 +77,7 @@ panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_ar
 // Register-resident panel (pm <= RPT * PANEL_THREADS): one barrier per column;
 // dynamic shared memory panel_regs_smem_bytes<T, RPT>().
 // two CTAs per SM unless the panel rows alone need more than 64 registers
-template <typename T, int RPT>
+template <typename T, int RPT, bool NOPIV = false>
 __global__ void __launch_bounds__(PANEL_THREADS, (sizeof(T) * RPT * PANEL_NB / 4 > 64) ? 1 : 2)
 panel_regs_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
                   int *info_array, StepSizes vs)
@@ -90,8 +90,8 @@ panel_regs_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ip
         return;
     }
     T *A = dA_array[mat] + j0 + (size_t)j0 * ldda;
-    const int info_local = panel_factor_regs<T, RPT>(m - j0, ib, A, ldda, s_ipiv, j0, smem);
-    if (tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
+    const int info_local = panel_factor_regs<T, RPT, NOPIV>(m - j0, ib, A, ldda, s_ipiv, j0, smem);
+    if (ipiv_array && tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
     if (tid == 0) {
         if (j0 == 0) info_array[mat] = info_local;
         else if (info_local != 0 && info_array[mat] == 0) info_array[mat] = info_local;
@@ -139,7 +139,11 @@ swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipi
         right = true;
         if (c0 >= n) return;             // past this matrix's columns
     }
-    if (threadIdx.x < 32) build_permutation(ipiv_array[mat], j0, ib, s_row, s_src, &s_cnt);
+    if (ipiv_array == nullptr) {             // no pivoting: no interchanges
+        if (threadIdx.x == 0) s_cnt = 0;
+    } else if (threadIdx.x < 32) {
+        build_permutation(ipiv_array[mat], j0, ib, s_row, s_src, &s_cnt);
+    }
     __syncthreads();
     apply_permutation<T>(A, ldda, c0, c1, s_row, s_src, s_cnt, s_tmp);
     if (right) trsm_l11_smem<T>(A, ldda, j0, ib, c0, c1, s_rhs, SWAP_COLS);
@@ -169,6 +173,26 @@ int blocked_panel_width(int m, int n, int j0)
     return panel_width<T>(m - j0, want, PANEL_SMEM_MAX);
 }
 
+// The panel kernel for panels of rpt rows per thread (0: shared memory).
+template <typename T, bool NOPIV>
+static void launch_panel(int rpt, int m, int n, int j0, int ib, T **dA, int ldda, int **ipiv,
+                         int *info, StepSizes vs, int nb, size_t smem, cudaStream_t s)
+{
+    if (rpt == 1)
+        MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 1, NOPIV><<<nb, PANEL_THREADS, smem, s>>>(
+            m, n, j0, ib, dA, ldda, ipiv, info, vs));
+    else if (rpt == 2)
+        MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 2, NOPIV><<<nb, PANEL_THREADS, smem, s>>>(
+            m, n, j0, ib, dA, ldda, ipiv, info, vs));
+    else if (rpt == 4)
+        MLU_LAUNCH(mlu::KC_PANEL, s,
+                   panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2), NOPIV><<<nb, PANEL_THREADS, smem, s>>>(
+                       m, n, j0, ib, dA, ldda, ipiv, info, vs));
+    else
+        MLU_LAUNCH(mlu::KC_PANEL, s, panel_kernel<T, NOPIV><<<nb, PANEL_THREADS, smem, s>>>(
+            m, n, j0, ib, dA, ldda, ipiv, info, vs));
+}
+
 // One step of the blocked factorisation for every matrix: panel at column j0
 // of width ib, interchanges + TRSM, and (when `update`) the trailing update.
 // `vsz`: per-matrix sizes of a variable-size batch (m, n = their maxima).
@@ -181,10 +205,14 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
     constexpr int BM = 64, BN = 64, TM = 4, TN = 4;
     static size_t panel_dyn_max = 0;
     if (!panel_dyn_max) {
-        panel_dyn_max = mlu_allow_dynamic_smem(panel_kernel<T>);
-        mlu_allow_dynamic_smem(panel_regs_kernel<T, 1>);
-        mlu_allow_dynamic_smem(panel_regs_kernel<T, 2>);
-        mlu_allow_dynamic_smem(panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2)>);
+        panel_dyn_max = min(mlu_allow_dynamic_smem(panel_kernel<T, false>),
+                            mlu_allow_dynamic_smem(panel_kernel<T, true>));
+        mlu_allow_dynamic_smem(panel_regs_kernel<T, 1, false>);
+        mlu_allow_dynamic_smem(panel_regs_kernel<T, 2, false>);
+        mlu_allow_dynamic_smem(panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2), false>);
+        mlu_allow_dynamic_smem(panel_regs_kernel<T, 1, true>);
+        mlu_allow_dynamic_smem(panel_regs_kernel<T, 2, true>);
+        mlu_allow_dynamic_smem(panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2), true>);
     }
     const int pm = m - j0;
     const int rpt = panel_rows_per_thread<T>(pm);
@@ -197,7 +225,7 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
         T **dAb = dA + b0;
-        int **ipb = ipiv + b0;
+        int **ipb = ipiv ? ipiv + b0 : nullptr;
         int *infb = info + b0;
         StepSizes vs = vsz;
         if (vs.m_arr) {
@@ -207,19 +235,11 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
         }
         // panel (one CTA per matrix), then interchanges + TRSM (one CTA per
         // matrix and 64-column tile)
-        if (rpt == 1)
-            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 1><<<nb, PANEL_THREADS, smem, s>>>(
-                m, n, j0, ib, dAb, ldda, ipb, infb, vs));
-        else if (rpt == 2)
-            MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 2><<<nb, PANEL_THREADS, smem, s>>>(
-                m, n, j0, ib, dAb, ldda, ipb, infb, vs));
-        else if (rpt == 4)
-            MLU_LAUNCH(mlu::KC_PANEL, s,
-                       panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2)><<<nb, PANEL_THREADS, smem, s>>>(
-                           m, n, j0, ib, dAb, ldda, ipb, infb, vs));
+        // no pivot array: LU without pivoting (the diagonal is the pivot)
+        if (ipiv == nullptr)
+            launch_panel<T, true>(rpt, m, n, j0, ib, dAb, ldda, nullptr, infb, vs, nb, smem, s);
         else
-            MLU_LAUNCH(mlu::KC_PANEL, s, panel_kernel<T><<<nb, PANEL_THREADS, smem, s>>>(
-                m, n, j0, ib, dAb, ldda, ipb, infb, vs));
+            launch_panel<T, false>(rpt, m, n, j0, ib, dAb, ldda, ipb, infb, vs, nb, smem, s);
         const int ncl = (j0 + SWAP_COLS - 1) / SWAP_COLS;
         const int ncr = (n - j0 - ib + SWAP_COLS - 1) / SWAP_COLS;
         if (ncl + ncr > 0)
@@ -313,7 +333,7 @@ getrs_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T **dB_a
     const int c0 = blockIdx.x * NR;
     const int nr = min(NR, nrhs - c0);
     const T *A = dA_array[mat];
-    const int *ipiv = ipiv_array[mat];
+    const int *ipiv = ipiv_array ? ipiv_array[mat] : nullptr;   // null: no interchanges
     T *B = dB_array[mat] + (size_t)c0 * lddb;
 
     for (int e = tid; e < NR * n; e += blockDim.x) {
@@ -352,7 +372,7 @@ magma_int_t blocked_getrs(bool trans, int n, int nrhs, T **dA, int ldda, int **i
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
         const dim3 grid((nrhs + nr - 1) / nr, nb);
         T **A = dA + b0, **B = dB + b0;
-        int **P = ipiv + b0;
+        int **P = ipiv ? ipiv + b0 : nullptr;
         if (trans && nr == 4)
             MLU_LAUNCH(mlu::KC_GETRS, s, getrs_kernel<T, true, 4><<<grid, threads, smem, s>>>(
                 n, nrhs, A, ldda, P, B, lddb));

@@ -21,6 +21,10 @@ constexpr int SWAP_W = 32;            // columns per gather/scatter chunk
 constexpr int GEMM_LDU = PANEL_NB + 4; // row stride of the transposed U12 tile in gemm_tile
 
 // ---------------------------------------------------------------------------
+// NOPIV (both panels): the pivot of column k is the diagonal entry, as in
+// MAGMA's getrf_nopiv; a zero diagonal sets info and leaves the column
+// unscaled, the same rule as a zero pivot column with pivoting.
+//
 // Panel factorisation of the pm x ib block at A (leading dimension lda) in
 // shared memory.  `smem` must hold pm*(ib+1) T plus 2*pm ints.  Every thread
 // of the block calls it.  On return the panel is written back in pivoted
@@ -34,7 +38,7 @@ constexpr int GEMM_LDU = PANEL_NB + 4; // row stride of the transposed U12 tile 
 // NaN rule), one warp combines the warp winners and updates the maps, then
 // every thread scales and updates only its own rows -- two barriers per
 // column.
-template <typename T>
+template <typename T, bool NOPIV = false>
 __device__ __forceinline__ int panel_factor(int pm, int ib, T *A, int lda, unsigned char *smem, int *s_ipiv,
                             int col0)
 {
@@ -63,6 +67,7 @@ __device__ __forceinline__ int panel_factor(int pm, int ib, T *A, int lda, unsig
                 const T v = sP[i * LDS + k];
                 unsigned long long mag = Prec<T>::absbits(v);
                 if (Prec<T>::isnan_(v)) mag = (p == k) ? 0x7fffffffffffffffull : 0ull;
+                if (NOPIV) mag = (p == k) ? 0x7fffffffffffffffull : 0ull;   // the diagonal
                 const unsigned long long key = mag | 0x8000000000000000ull;
                 if (key > best || (key == best && (unsigned)p < bpos)) { best = key; bpos = p; }
             }
@@ -149,7 +154,7 @@ __host__ __device__ constexpr size_t panel_regs_smem_bytes()
            (size_t)panel_regs_ld<T, RPT>() * sizeof(int);
 }
 
-template <typename T, int RPT>
+template <typename T, int RPT, bool NOPIV = false>
 __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, int *s_ipiv,
                                                  int col0, unsigned char *smem)
 {
@@ -188,6 +193,7 @@ __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, 
                 const T v = a[r][0];
                 unsigned long long mag = Prec<T>::absbits(v);
                 if (Prec<T>::isnan_(v)) mag = (pos[r] == k) ? 0x7fffffffffffffffull : 0ull;
+                if (NOPIV) mag = (pos[r] == k) ? 0x7fffffffffffffffull : 0ull;   // the diagonal
                 const unsigned long long key = mag | 0x8000000000000000ull;
                 if (key > best || (key == best && (unsigned)pos[r] < bpos)) {
                     best = key; bpos = pos[r]; bslot = r;

@@ -108,6 +108,20 @@ for _p in "ds":
                                                    c_int, c_ptr, c_int, c_int, c_int, c_ptr], c_int)
     _PROTOS[f"magma_{_p}gesv_batched_strided"] = ([c_int, c_int, c_ptr, c_int, c_int, c_ptr, c_int,
                                                   c_ptr, c_int, c_int, c_ptr, c_int, c_ptr], c_int)
+for _p in "ds":
+    _PROTOS[f"magma_{_p}getrf_nopiv_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr],
+                                                 c_int)
+    _PROTOS[f"magma_{_p}getrs_nopiv_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int,
+                                                  c_ptr, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}gesv_nopiv_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr,
+                                                 c_int, c_ptr], c_int)
+_PROTOS["magma_dgerbt_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, c_ptr,
+                                    c_ptr, c_int, c_ptr], c_int)
+_PROTOS["magmablas_dprbt_batched"] = ([c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, c_ptr], None)
+_PROTOS["magmablas_dprbt_mtv_batched"] = ([c_int, c_int, c_ptr, c_ptr, c_int, c_int, c_ptr], None)
+_PROTOS["magmablas_dprbt_mv_batched"] = ([c_int, c_int, c_ptr, c_ptr, c_int, c_int, c_ptr], None)
+_PROTOS["magma_dgesv_rbt_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr],
+                                      c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
 _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],

@@ -66,14 +66,15 @@ static int P##_iamax(int len, const T *a, int inc)                              
     return best;                                                                       \
 }                                                                                      \
                                                                                        \
-int oracle_##P##getrf(int m, int n, T *A, int lda, int *ipiv)                          \
+/* nopiv: the diagonal is the pivot (MAGMA's getrf_nopiv); ipiv may be NULL. */      \
+static int P##getrf_impl(int m, int n, T *A, int lda, int *ipiv, int nopiv)            \
 {                                                                                      \
     int info = 0;                                                                      \
     int mn = m < n ? m : n;                                                            \
     for (int k = 0; k < mn; k++) {                                                     \
         T *colk = A + (size_t)k * lda;                                                 \
-        int p = k + P##_iamax(m - k, colk + k, 1);                                     \
-        ipiv[k] = p + 1;                                                               \
+        int p = nopiv ? k : k + P##_iamax(m - k, colk + k, 1);                         \
+        if (ipiv) ipiv[k] = p + 1;                                                     \
         if (colk[p] != (T)0) {                                                         \
             if (p != k) {                                                              \
                 for (int j = 0; j < n; j++) {                                          \
@@ -94,6 +95,16 @@ int oracle_##P##getrf(int m, int n, T *A, int lda, int *ipiv)                   
         }                                                                              \
     }                                                                                  \
     return info;                                                                       \
+}                                                                                      \
+                                                                                       \
+int oracle_##P##getrf(int m, int n, T *A, int lda, int *ipiv)                          \
+{                                                                                      \
+    return P##getrf_impl(m, n, A, lda, ipiv, 0);                                       \
+}                                                                                      \
+                                                                                       \
+int oracle_##P##getrf_nopiv(int m, int n, T *A, int lda)                               \
+{                                                                                      \
+    return P##getrf_impl(m, n, A, lda, NULL, 1);                                       \
 }                                                                                      \
                                                                                        \
 void oracle_##P##getrs(int trans, int n, int nrhs, const T *LU, int lda,               \
@@ -444,3 +455,91 @@ void oracle_##P##gesv_adjoint_batched(int n, int nrhs, const T *LU, int lda, lon
 }
 DEFINE_ADJOINT(double, d, fma)
 DEFINE_ADJOINT(float, s, fmaf)
+
+/* Random butterfly transformation, the GPU's arithmetic (magma_gb300/csrc
+ * rbt.cu, restating the depth-2 RBT of the reference's magma_dgerbt_batched):
+ * level 0 is one butterfly of order n, level 1 two of orders ceil(n/2) and
+ * n - ceil(n/2); a block of order m pairs (i, i + m/2), the last index of an
+ * odd block is unpaired; R = w[base + k], S = w[base + k + m/2] with base 0
+ * (level 0) or n + block start (level 1); c = 1/sqrt 2. */
+static const double RBT_C = 0.70710678118654752440;
+
+static void rbt_block(int level, int n, int x, int *b0, int *g)
+{
+    if (level == 0) { *b0 = 0; *g = n / 2; return; }
+    int n1 = (n + 1) / 2;
+    if (x < n1) { *b0 = 0; *g = n1 / 2; } else { *b0 = n1; *g = (n - n1) / 2; }
+}
+
+/* A <- U^T A V one level at a time (inner, then outer); per 2x2 group the
+ * column transform first, then the row transform. */
+void oracle_rbt_matrix(int n, double *A, int lda, const double *u, const double *v)
+{
+    for (int level = 1; level >= 0; level--) {
+        for (int ri = 0; ri < n; ri++) {
+            int rb0, rg;
+            rbt_block(level, n, ri, &rb0, &rg);
+            int ki = ri - rb0;
+            if (ki >= rg && ki != 2 * rg) continue;      /* bottoms are handled with their tops */
+            int rpair = ki < rg, ri2 = ri + rg;
+            for (int cj = 0; cj < n; cj++) {
+                int cb0, cg;
+                rbt_block(level, n, cj, &cb0, &cg);
+                int kj = cj - cb0;
+                if (kj >= cg && kj != 2 * cg) continue;
+                int cpair = kj < cg, cj2 = cj + cg;
+                double a = A[ri + (size_t)cj * lda];
+                double b = cpair ? A[ri + (size_t)cj2 * lda] : 0.0;
+                double c = rpair ? A[ri2 + (size_t)cj * lda] : 0.0;
+                double d = (rpair && cpair) ? A[ri2 + (size_t)cj2 * lda] : 0.0;
+                if (cpair) {
+                    int vb = (level == 0 ? 0 : n + cb0) + kj;
+                    double wr = RBT_C * v[vb], ws = RBT_C * v[vb + cg];
+                    double a1 = wr * (a + b), b1 = ws * (a - b);
+                    double c1 = wr * (c + d), d1 = ws * (c - d);
+                    a = a1; b = b1; c = c1; d = d1;
+                }
+                if (rpair) {
+                    int ub = (level == 0 ? 0 : n + rb0) + ki;
+                    double wr = RBT_C * u[ub], ws = RBT_C * u[ub + rg];
+                    double a1 = wr * (a + c), c1 = ws * (a - c);
+                    double b1 = wr * (b + d), d1 = ws * (b - d);
+                    a = a1; c = c1; b = b1; d = d1;
+                }
+                A[ri + (size_t)cj * lda] = a;
+                if (cpair) A[ri + (size_t)cj2 * lda] = b;
+                if (rpair) A[ri2 + (size_t)cj * lda] = c;
+                if (rpair && cpair) A[ri2 + (size_t)cj2 * lda] = d;
+            }
+        }
+    }
+}
+
+/* trans: B <- U^T B (inner level, then outer); else B <- V B (outer, then
+ * inner). */
+void oracle_rbt_vectors(int trans, int n, int nrhs, const double *w, double *B, int ldb)
+{
+    for (int step = 0; step < 2; step++) {
+        int level = trans ? 1 - step : step;
+        for (int col = 0; col < nrhs; col++) {
+            double *x = B + (size_t)col * ldb;
+            for (int ri = 0; ri < n; ri++) {
+                int b0, g;
+                rbt_block(level, n, ri, &b0, &g);
+                int k = ri - b0;
+                if (k >= g) continue;
+                int wb = (level == 0 ? 0 : n + b0) + k;
+                double R = w[wb], S = w[wb + g];
+                double xt = x[ri], yb = x[ri + g];
+                if (trans) {
+                    x[ri] = (RBT_C * R) * (xt + yb);
+                    x[ri + g] = (RBT_C * S) * (xt - yb);
+                } else {
+                    double p = R * xt, q = S * yb;
+                    x[ri] = RBT_C * (p + q);
+                    x[ri + g] = RBT_C * (p - q);
+                }
+            }
+        }
+    }
+}

@@ -215,6 +215,43 @@ def dsgesv_batched(A, B, itermax=30, tol=0.0, fallback=True, nthreads=None):
     return X, ipiv, info, iters
 
 
+def getrf_nopiv(A2, m=None):
+    """LU without pivoting of one matrix, (ncols, ld) storage, in place.  Returns info."""
+    lib = load()
+    n, ld = A2.shape
+    m = n if m is None else m
+    fn = getattr(lib, "oracle_dgetrf_nopiv" if A2.dtype == np.float64 else "oracle_sgetrf_nopiv")
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int]
+    assert A2.flags.c_contiguous
+    return int(fn(m, n, _p(A2), ld))
+
+
+def rbt_matrix(A2, u, v):
+    """A <- U^T A V (oracle_rbt_matrix) on one (n, ld) FP64 storage array, in place."""
+    lib = load()
+    n, ld = A2.shape
+    fn = lib.oracle_rbt_matrix
+    fn.restype = None
+    fn.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    fn(n, _p(A2), ld, _p(u), _p(v))
+    return A2
+
+
+def rbt_vectors(trans, B2, w, n):
+    """B <- U^T B (trans) or V B on one (nrhs, ld) FP64 storage array, in place."""
+    lib = load()
+    nrhs, ld = B2.shape
+    fn = lib.oracle_rbt_vectors
+    fn.restype = None
+    fn.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    fn(1 if trans else 0, n, nrhs, _p(w), _p(B2), ld)
+    return B2
+
+
 def getri(LU, ipiv):
     """Inverse from the LU factors, the GPU's order: Y = solve(L, U, I) column by column
     (getrs arithmetic, no interchanges), then column j of Y is column perm[j] of inv(A), perm
