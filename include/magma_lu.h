@@ -65,6 +65,11 @@ typedef enum {
     MagmaTrue  = 1
 } magma_bool_t;                       /* include/magma_types.h:600-603 */
 
+typedef enum {
+    MagmaUpper = 121,
+    MagmaLower = 122
+} magma_uplo_t;                       /* include/magma_types.h:619-623 (MagmaFull omitted) */
+
 /* ------------------------------------------------------------------------ */
 /* Runtime subset -- include/magma_auxiliary.h:24-25, 82-105, 258-330, 357 */
 
@@ -617,6 +622,34 @@ magma_int_t magma_dgesv_rbt_batched(magma_int_t n, magma_int_t nrhs, double **dA
                                     magma_int_t ldda, double **dB_array, magma_int_t lddb,
                                     magma_int_t *dinfo_array, magma_int_t batchCount,
                                     magma_queue_t queue);
+
+/* Cholesky A = L L^T of symmetric positive definite matrices and the solve
+ * (include/magma_zbatched.h: magma_zpotrf_batched, magma_zpotrs_batched,
+ * magma_zposv_batched; src/zpotrf_batched.cpp:96-170).  Lower triangle only;
+ * MagmaUpper returns -1 after magma_xerbla, as in the reference.  info = j
+ * (1-based) for the first non-positive (or NaN) pivot; that matrix is left
+ * as it was at that point.  The strictly upper triangle is never written.  No
+ * allocation, no synchronisation. */
+magma_int_t magma_dpotrf_batched(magma_uplo_t uplo, magma_int_t n, double **dA_array,
+                                 magma_int_t ldda, magma_int_t *info_array,
+                                 magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_spotrf_batched(magma_uplo_t uplo, magma_int_t n, float **dA_array,
+                                 magma_int_t ldda, magma_int_t *info_array,
+                                 magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_dpotrs_batched(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs,
+                                 double **dA_array, magma_int_t ldda, double **dB_array,
+                                 magma_int_t lddb, magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_spotrs_batched(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs,
+                                 float **dA_array, magma_int_t ldda, float **dB_array,
+                                 magma_int_t lddb, magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_dposv_batched(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs,
+                                double **dA_array, magma_int_t ldda, double **dB_array,
+                                magma_int_t lddb, magma_int_t *dinfo_array,
+                                magma_int_t batchCount, magma_queue_t queue);
+magma_int_t magma_sposv_batched(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs,
+                                float **dA_array, magma_int_t ldda, float **dB_array,
+                                magma_int_t lddb, magma_int_t *dinfo_array,
+                                magma_int_t batchCount, magma_queue_t queue);
 
 /* ------------------------------------------------------------------------
  * Tuning of the variable-size kernel.  No counterpart in the reference, whose

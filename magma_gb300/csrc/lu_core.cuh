@@ -407,7 +407,11 @@ __device__ __forceinline__ void trsm_l11_smem(T *A, int lda, int j0, int ib, int
 // acc = fma(-l_k, u_k, acc) for k ascending.  The U12 tile is stored
 // transposed (sU[j][k]) so that its store (lanes down a column of A) and the
 // compute loop's reads (4 consecutive k per thread) are free of bank conflicts.
-template <typename T, int BM, int BN, int TM, int TN>
+//
+// SYRK (the Cholesky trailing update A22 -= L21 L21^T): U12 is L21^T, read
+// from the rows c0.. of the panel columns, and only elements on or below the
+// diagonal (row >= column) are stored.
+template <typename T, int BM, int BN, int TM, int TN, bool SYRK = false>
 __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, int ib, int r0, int c0, T *sL,
                           T *sU)
 {
@@ -423,14 +427,17 @@ __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, i
             const int e = tid + u * NT;
             const int i = e % BM, kl = e / BM;
             vl[u] = (kl < ib && r0 + i < m) ? A[r0 + i + (size_t)(j0 + kl) * lda] : T(0);
-            const int ku = e % ib, j = e / ib;
-            vu[u] = (e < ib * BN && c0 + j < n) ? A[j0 + ku + (size_t)(c0 + j) * lda] : T(0);
+            const int ku = SYRK ? e / BN : e % ib, j = SYRK ? e % BN : e / ib;
+            vu[u] = (e < ib * BN && c0 + j < n)
+                        ? (SYRK ? A[c0 + j + (size_t)(j0 + ku) * lda] : A[j0 + ku + (size_t)(c0 + j) * lda])
+                        : T(0);
         }
 #pragma unroll
         for (int u = 0; u < LU_LOADS; u++) {
             const int e = tid + u * NT;
             if (e < ib * BM) sL[(e / BM) * BM + e % BM] = vl[u];
-            if (e < ib * BN) sU[(e / ib) * GEMM_LDU + e % ib] = vu[u];
+            const int ku = SYRK ? e / BN : e % ib, j = SYRK ? e % BN : e / ib;
+            if (e < ib * BN) sU[j * GEMM_LDU + ku] = vu[u];
         }
     }
     const int tr = tid % (BM / TM), tc = tid / (BM / TM);
@@ -481,7 +488,7 @@ __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, i
 #pragma unroll
         for (int a = 0; a < TM; a++) {
             const int r = r0 + tr * TM + a;
-            if (r < m && c < n) A[r + (size_t)c * lda] = acc[a][b];
+            if (r < m && c < n && (!SYRK || r >= c)) A[r + (size_t)c * lda] = acc[a][b];
         }
     }
 }

@@ -122,6 +122,12 @@ _PROTOS["magmablas_dprbt_mtv_batched"] = ([c_int, c_int, c_ptr, c_ptr, c_int, c_
 _PROTOS["magmablas_dprbt_mv_batched"] = ([c_int, c_int, c_ptr, c_ptr, c_int, c_int, c_ptr], None)
 _PROTOS["magma_dgesv_rbt_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr],
                                       c_int)
+for _p in "ds":
+    _PROTOS[f"magma_{_p}potrf_batched"] = ([c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}potrs_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_int,
+                                            c_ptr], c_int)
+    _PROTOS[f"magma_{_p}posv_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr,
+                                           c_int, c_ptr], c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
 _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],

@@ -543,3 +543,75 @@ void oracle_rbt_vectors(int trans, int n, int nrhs, const double *w, double *B, 
         }
     }
 }
+
+/* Cholesky A = L L^T (lower) and its solve, the GPU's order (magma_gb300/csrc
+ * chol.cu; the reference's magma_?potrf_batched / potrs / posv): 32-column
+ * panels; per panel the diagonal block right-looking (l_kk = sqrt(a_kk),
+ * column below scaled by 1/l_kk with the sfmin rule, a_it = fma(-l_ik, l_tk,
+ * a_it) for i >= t > k), then every row below solved against L11 (k
+ * ascending), then A22 -= L21 L21^T on the lower triangle (k ascending).  A
+ * pivot that is not > 0 (or NaN) at column j returns info = j + 1 at once,
+ * the diagonal block left as updated so far.  Solve: L y = b then L^T x = y,
+ * each with the diagonal multiplied in as a reciprocal. */
+#define DEFINE_CHOL(T, P, FMA, SQRT)                                                        \
+int oracle_##P##potrf(int n, T *A, int lda)                                                 \
+{                                                                                           \
+    for (int j0 = 0; j0 < n; j0 += 32) {                                                    \
+        int ib = n - j0 < 32 ? n - j0 : 32;                                                 \
+        for (int k = 0; k < ib; k++) {                                                      \
+            T d = A[(j0 + k) + (size_t)(j0 + k) * lda];                                     \
+            if (!(d > (T)0)) return j0 + k + 1;                                             \
+            T s = SQRT(d), r = (T)1 / s;                                                    \
+            A[(j0 + k) + (size_t)(j0 + k) * lda] = s;                                       \
+            for (int i = k + 1; i < ib; i++) {                                              \
+                T *x = &A[(j0 + i) + (size_t)(j0 + k) * lda];                               \
+                *x = P##_rscale(*x, s, r);                                                  \
+            }                                                                               \
+            for (int t = k + 1; t < ib; t++) {                                              \
+                T ltk = A[(j0 + t) + (size_t)(j0 + k) * lda];                               \
+                for (int i = t; i < ib; i++) {                                              \
+                    T *x = &A[(j0 + i) + (size_t)(j0 + t) * lda];                           \
+                    *x = FMA(-A[(j0 + i) + (size_t)(j0 + k) * lda], ltk, *x);               \
+                }                                                                           \
+            }                                                                               \
+        }                                                                                   \
+        for (int i = j0 + ib; i < n; i++)                                                   \
+            for (int k = 0; k < ib; k++) {                                                  \
+                T lkk = A[(j0 + k) + (size_t)(j0 + k) * lda];                               \
+                T *xk = &A[i + (size_t)(j0 + k) * lda];                                     \
+                *xk = P##_rscale(*xk, lkk, (T)1 / lkk);                                     \
+                for (int t = k + 1; t < ib; t++) {                                          \
+                    T *xt = &A[i + (size_t)(j0 + t) * lda];                                 \
+                    *xt = FMA(-*xk, A[(j0 + t) + (size_t)(j0 + k) * lda], *xt);             \
+                }                                                                           \
+            }                                                                               \
+        for (int c = j0 + ib; c < n; c++)                                                   \
+            for (int r = c; r < n; r++) {                                                   \
+                T acc = A[r + (size_t)c * lda];                                             \
+                for (int k = 0; k < ib; k++)                                                \
+                    acc = FMA(-A[r + (size_t)(j0 + k) * lda], A[c + (size_t)(j0 + k) * lda], \
+                              acc);                                                         \
+                A[r + (size_t)c * lda] = acc;                                               \
+            }                                                                               \
+    }                                                                                       \
+    return 0;                                                                               \
+}                                                                                           \
+                                                                                            \
+void oracle_##P##potrs(int n, int nrhs, const T *L, int lda, T *B, int ldb)                 \
+{                                                                                           \
+    for (int c = 0; c < nrhs; c++) {                                                        \
+        T *b = B + (size_t)c * ldb;                                                         \
+        for (int t = 0; t < n; t++) {                                                       \
+            T d = L[t + (size_t)t * lda];                                                   \
+            b[t] = P##_rscale(b[t], d, (T)1 / d);                                           \
+            for (int i = t + 1; i < n; i++) b[i] = FMA(-L[i + (size_t)t * lda], b[t], b[i]); \
+        }                                                                                   \
+        for (int t = n - 1; t >= 0; t--) {                                                  \
+            T d = L[t + (size_t)t * lda];                                                   \
+            b[t] = P##_rscale(b[t], d, (T)1 / d);                                           \
+            for (int i = 0; i < t; i++) b[i] = FMA(-L[t + (size_t)i * lda], b[t], b[i]);    \
+        }                                                                                   \
+    }                                                                                       \
+}
+DEFINE_CHOL(double, d, fma, sqrt)
+DEFINE_CHOL(float, s, fmaf, sqrtf)

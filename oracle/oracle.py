@@ -252,6 +252,28 @@ def rbt_vectors(trans, B2, w, n):
     return B2
 
 
+def potrf(A2):
+    """Lower Cholesky of one (n, ld) storage array in place (oracle_?potrf).  Returns info."""
+    lib = load()
+    n, ld = A2.shape
+    fn = getattr(lib, "oracle_dpotrf" if A2.dtype == np.float64 else "oracle_spotrf")
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int, C.c_void_p, C.c_int]
+    return int(fn(n, _p(A2), ld))
+
+
+def potrs(L2, B2):
+    """Solve L L^T X = B in place (oracle_?potrs); L2 (n, ld), B2 (nrhs, ldb) storage."""
+    lib = load()
+    n, ld = L2.shape
+    nrhs, ldb = B2.shape
+    fn = getattr(lib, "oracle_dpotrs" if L2.dtype == np.float64 else "oracle_spotrs")
+    fn.restype = None
+    fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int]
+    fn(n, nrhs, _p(L2), ld, _p(B2), ldb)
+    return B2
+
+
 def getri(LU, ipiv):
     """Inverse from the LU factors, the GPU's order: Y = solve(L, U, I) column by column
     (getrs arithmetic, no interchanges), then column j of Y is column perm[j] of inv(A), perm
