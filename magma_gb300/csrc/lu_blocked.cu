@@ -8,19 +8,23 @@
 // trailing update magmablas/zgemm_batched.cpp:50-97 -> cublasDgemmBatched)
 // and the n > 32 part of magma_dgetrs_batched (src/zgetrs_batched.cpp:86-181).
 //
-// One step of panel width ib at column j0 is three launches:
+// One step of panel width ib at column j0 is two or three launches:
 //   panel_kernel      one CTA per matrix: the (m-j0) x ib panel is staged in
-//                     shared memory and factored column by column (lazy row
-//                     interchange, pivot search on the integer pipes), then
+//                     shared memory or registers and factored column by
+//                     column (pivot search on the integer pipes), then
 //                     written back in pivoted order with its pivots;
-//   swap_trsm_kernel  one CTA per (matrix, 32-column tile) outside the panel:
-//                     applies the panel's interchanges to the tile and, right
-//                     of the panel, solves L11 U12 = A12 with one thread per
-//                     column;
-//   gemm_kernel       one CTA per (matrix, 64x64 tile of A22): A22 -= L21 U12,
-//                     one accumulator per element seeded with A22 and updated
-//                     in increasing k, so the result is bit-identical to the
-//                     unblocked elimination order.
+//   band_kernel       (FP32, large batches) one CTA per (matrix, 64-column
+//                     band right of the panel): the panel's interchanges, the
+//                     solve L11 U12 = A12 and A22 -= L21 U12 for every row
+//                     tile of the band, U12 kept in shared memory;
+//   swap_trsm_kernel  otherwise, one CTA per (matrix, 64-column tile):
+//     + gemm_kernel   interchanges and U12, then one CTA per 64x64 tile of
+//                     A22 for the update.
+// Every element is updated with one accumulator in increasing k, so the
+// result is bit-identical to the unblocked elimination order.  The
+// interchanges left of each panel are applied after the last step by
+// left_swaps_kernel (one coalesced gather per earlier panel) when the matrix
+// has at most 1024 rows, else by swap_trsm_kernel in each step.
 // No workspace and no host synchronisation: every call is stream-ordered and
 // capturable in a CUDA graph.
 #include "common.cuh"
@@ -101,7 +105,7 @@ panel_regs_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ip
 // Rows per thread of the register-resident panel for pm rows, 0 when the
 // panel is too tall for registers (FP64: 512 rows, FP32: 1024 rows).
 template <typename T>
-int panel_rows_per_thread(int pm)
+__host__ __device__ inline int panel_rows_per_thread(int pm)
 {
     if (pm <= PANEL_THREADS) return 1;
     if (pm <= 2 * PANEL_THREADS) return 2;
@@ -117,7 +121,7 @@ constexpr int SWAP_COLS = 64;
 template <typename T>
 __global__ void __launch_bounds__(SWAP_THREADS)
 swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
-                 StepSizes vs)
+                 StepSizes vs, int with_left)
 {
     __shared__ int s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt;
     __shared__ T s_tmp[2 * PANEL_NB * (SWAP_W + 1)];
@@ -126,7 +130,7 @@ swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipi
     if (!vs.get(mat, j0, m, n, ldda, ib)) return;
     T *A = dA_array[mat];
     // column tile: left tiles cover [0, j0), right tiles cover [j0+ib, n)
-    const int nleft = (j0 + SWAP_COLS - 1) / SWAP_COLS;
+    const int nleft = with_left ? (j0 + SWAP_COLS - 1) / SWAP_COLS : 0;
     int c0, c1;
     bool right;
     if ((int)blockIdx.x < nleft) {
@@ -163,10 +167,385 @@ gemm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int tiles_m, S
                                  j0 + ib + tn * BN, sL, sU);
 }
 
+// ---------------------------------------------------------------------------
+// The step right of the panel in one launch: one CTA per (matrix, BAND_N-column
+// band of columns j0+ib..n).
+//   1. the step's interchanges as a table of touched rows (build_permutation);
+//   2. the band's original top rows (rows j0..j0+ib) and L11 staged in shared
+//      memory, coalesced;
+//   3. the interchanged top rows, i.e. U12 before the solve: a top row's new
+//      content is an original top row (from shared memory) or a row further
+//      down (the only scattered reads: at most ib rows of the band);
+//   4. U12 = L11^{-1} U12 in registers, one thread per column, written back;
+//   5. every BAND_M-row tile below: A22 -= L21 U12 with U12 from shared
+//      memory.  A row that receives an original top row in this step's
+//      interchanges (always a top row: each interchange k moves row j0+k, which
+//      still holds an original top row, down) takes its value from shared
+//      memory, so the interchanges need no scattered writes.
+// Per element the same operations, in the same order, as swap_trsm_kernel
+// followed by gemm_kernel.  Columns left of the panel are not touched (their
+// interchanges are applied by swap_trsm_kernel or, after the last step, by
+// left_swaps_kernel).
+template <typename T>
+__host__ __device__ int blocked_panel_width(int m, int n, int j0);
+
+constexpr int BAND_N = 64, BAND_M = 64, BAND_TM = 4, BAND_TN = 4;
+constexpr int BAND_THREADS = (BAND_M / BAND_TM) * (BAND_N / BAND_TN);
+constexpr int BAND_TOP_LD = BAND_N + 1;
+constexpr int BAND_LOADS = PANEL_NB * BAND_N / BAND_THREADS;   // per thread, 8
+static_assert(BAND_M == BAND_N && BAND_LOADS * BAND_THREADS == PANEL_NB * BAND_N, "band tiling");
+
+// The band kernel is used for FP32 only.  In FP64 its one-warp-pair TRSM
+// prologue runs on the FP64 pipe while the CTA's other warps wait, and the
+// separate interchange/TRSM and update kernels were faster on GB300 (79.4 ms
+// against 85.6 ms for the variable-size FP64 solve of 256 matrices of order
+// 128..1024; 10.44 ms against 10.76 ms for the FP32 factorisation of 512
+// matrices of order 512 inside the refinement).
+template <typename T>
+__host__ __device__ constexpr bool band_used() { return sizeof(T) == 4; }
+
+// FP32: the tiles' A22 and L21 blocks are double-buffered in shared memory
+// (cp.async), so a tile's loads overlap the previous tile's FMAs.  FP64 keeps
+// one L21 buffer and loads A22 into registers (its FMA rate, not latency,
+// bounds it, and the buffers would leave one CTA per SM).
+template <typename T>
+__host__ __device__ constexpr bool band_pipelined() { return sizeof(T) == 4; }
+
+template <typename T>
+__host__ __device__ constexpr size_t band_smem_bytes()
+{
+    return sizeof(T) * ((size_t)BAND_N * GEMM_LDU + (size_t)PANEL_NB * BAND_TOP_LD +
+                        (band_pipelined<T>() ? 2 * ((size_t)PANEL_NB * BAND_M + (size_t)BAND_M * BAND_N)
+                                             : (size_t)PANEL_NB * BAND_M));
+}
+
+// cp.async of one element (4 or 8 bytes) to shared memory; `valid` false
+// writes zeros and reads nothing (src must still be a valid address).
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void *dst, const void *src, bool valid)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(src), "n"(BYTES),
+                 "r"(valid ? BYTES : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename T>
+__global__ void __launch_bounds__(BAND_THREADS, sizeof(T) == 4 ? 3 : 2)
+band_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array, StepSizes vs)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr bool PIPE = band_pipelined<T>();
+    T *sU = reinterpret_cast<T *>(smem_raw);          // [BAND_N][GEMM_LDU]: U12, transposed
+    T *sTop = sU + BAND_N * GEMM_LDU;                 // [PANEL_NB][BAND_TOP_LD]: original top rows
+    T *sL = sTop + PANEL_NB * BAND_TOP_LD;            // [2][PANEL_NB][BAND_M]: L21 tiles (L11 first)
+    T *sAcc = sL + (PIPE ? 2 : 1) * PANEL_NB * BAND_M;   // [2][BAND_N][BAND_M]: A22 tiles (PIPE)
+    __shared__ int s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt, s_top_src[PANEL_NB];
+    __shared__ unsigned s_mask[2];
+    const int mat = blockIdx.y, tid = threadIdx.x;
+    if (!vs.get(mat, j0, m, n, ldda, ib)) return;
+    const int c0 = j0 + ib + blockIdx.x * BAND_N;
+    if (c0 >= n) return;                              // past this matrix's columns
+    const int w = min(BAND_N, n - c0);
+    T *A = dA_array[mat];
+    const size_t ld = ldda;
+    {
+        // original top rows of the band and L11: all loads in flight while warp 0
+        // builds the interchange table
+        T v[BAND_LOADS], l[PANEL_NB * PANEL_NB / BAND_THREADS];
+#pragma unroll
+        for (int u = 0; u < BAND_LOADS; u++) {
+            const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
+            v[u] = (k < ib && j < w) ? A[j0 + k + (size_t)(c0 + j) * ld] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < PANEL_NB * PANEL_NB / BAND_THREADS; u++) {
+            const int e = tid + u * BAND_THREADS, i = e % PANEL_NB, t = e / PANEL_NB;
+            l[u] = (i < ib && t < ib) ? A[j0 + i + (size_t)(j0 + t) * ld] : T(0);
+        }
+        if (tid < 32) {
+            if (ipiv_array == nullptr) {              // no pivoting: no interchanges
+                if (tid == 0) s_cnt = 0;
+            } else {
+                build_permutation(ipiv_array[mat], j0, ib, s_row, s_src, &s_cnt);
+            }
+            // where each top row's new content comes from (identity, then the
+            // table's entries inside the top block)
+            s_top_src[tid] = j0 + tid;
+            __syncwarp();
+            const int cnt = ipiv_array == nullptr ? 0 : s_cnt;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int e = tid + 32 * h;
+                if (e < cnt && s_row[e] < j0 + ib) s_top_src[s_row[e] - j0] = s_src[e];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < BAND_LOADS; u++) {
+            const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
+            sTop[k * BAND_TOP_LD + j] = v[u];
+        }
+#pragma unroll
+        for (int u = 0; u < PANEL_NB * PANEL_NB / BAND_THREADS; u++) {
+            const int e = tid + u * BAND_THREADS, i = e % PANEL_NB, t = e / PANEL_NB;
+            sL[i * (PANEL_NB + 1) + t] = l[u];         // L11[i][t]
+        }
+    }
+    __syncthreads();
+    {
+        T v[BAND_LOADS];
+#pragma unroll
+        for (int u = 0; u < BAND_LOADS; u++) {
+            const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
+            v[u] = T(0);
+            if (k < ib && j < w) {
+                const int src = s_top_src[k];
+                v[u] = src < j0 + ib ? sTop[(src - j0) * BAND_TOP_LD + j]
+                                     : A[src + (size_t)(c0 + j) * ld];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < BAND_LOADS; u++) {
+            const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
+            sU[j * GEMM_LDU + k] = v[u];
+        }
+    }
+    __syncthreads();
+    if (tid < w) {                                    // U12 = L11^{-1} U12, column tid
+        T x[PANEL_NB];
+#pragma unroll
+        for (int k = 0; k < PANEL_NB; k++) x[k] = sU[tid * GEMM_LDU + k];
+#pragma unroll
+        for (int t = 0; t < PANEL_NB; t++) {
+            if (t < ib) {
+#pragma unroll
+                for (int i = t + 1; i < PANEL_NB; i++)
+                    if (i < ib) x[i] = Prec<T>::fma_(-sL[i * (PANEL_NB + 1) + t], x[t], x[i]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < PANEL_NB; k++) sU[tid * GEMM_LDU + k] = x[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < BAND_LOADS; u++) {
+        const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
+        if (k < ib && j < w) A[j0 + k + (size_t)(c0 + j) * ld] = sU[j * GEMM_LDU + k];
+    }
+    const int tr = tid % (BAND_M / BAND_TM), tc = tid / (BAND_M / BAND_TM);
+    // copies of tile r0's A22 block ([c][r]) and L21 block ([k][r]) into buffer buf
+    auto issue = [&](int r0, int buf) {
+        T *dAcc = sAcc + buf * BAND_M * BAND_N, *dL = sL + buf * PANEL_NB * BAND_M;
+#pragma unroll
+        for (int u = 0; u < BAND_M * BAND_N / BAND_THREADS; u++) {
+            const int e = tid + u * BAND_THREADS, r = e % BAND_M, c = e / BAND_M;
+            const bool ok = r0 + r < m && c < w;
+            cp_async_elem<sizeof(T)>(dAcc + e, ok ? A + r0 + r + (size_t)(c0 + c) * ld : A, ok);
+        }
+#pragma unroll
+        for (int u = 0; u < BAND_LOADS; u++) {
+            const int e = tid + u * BAND_THREADS, i = e % BAND_M, kl = e / BAND_M;
+            const bool ok = kl < ib && r0 + i < m;
+            cp_async_elem<sizeof(T)>(dL + e, ok ? A + r0 + i + (size_t)(j0 + kl) * ld : A, ok);
+        }
+    };
+    __syncthreads();                                  // L11 no longer needed in sL
+    if (PIPE && j0 + ib < m) issue(j0 + ib, 0);
+    if (PIPE) cp_async_commit();
+    int buf = 0;
+    for (int r0 = j0 + ib; r0 < m; r0 += BAND_M, buf ^= 1) {
+        T acc[BAND_TM][BAND_TN];
+        const T *tL = sL + (PIPE ? buf * PANEL_NB * BAND_M : 0);
+        if (PIPE) {
+            if (r0 + BAND_M < m) issue(r0 + BAND_M, buf ^ 1);
+            cp_async_commit();
+            cp_async_wait<1>();                       // this tile's copies have landed
+        } else {
+            __syncthreads();                          // sL free again
+#pragma unroll
+            for (int b = 0; b < BAND_TN; b++) {
+                const int c = c0 + tc * BAND_TN + b;
+#pragma unroll
+                for (int a = 0; a < BAND_TM; a++) {
+                    const int r = r0 + tr * BAND_TM + a;
+                    acc[a][b] = (r < m && c < n) ? A[r + (size_t)c * ld] : T(0);
+                }
+            }
+            T vl[BAND_LOADS];
+#pragma unroll
+            for (int u = 0; u < BAND_LOADS; u++) {
+                const int e = tid + u * BAND_THREADS, i = e % BAND_M, kl = e / BAND_M;
+                vl[u] = (kl < ib && r0 + i < m) ? A[r0 + i + (size_t)(j0 + kl) * ld] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < BAND_LOADS; u++) sL[tid + u * BAND_THREADS] = vl[u];
+        }
+        if (tid < 32) {                               // touched rows inside this tile
+            const int cnt = s_cnt;
+            const bool in0 = tid < cnt && s_row[tid] >= r0 && s_row[tid] < r0 + BAND_M;
+            const bool in1 = tid + 32 < cnt && s_row[tid + 32] >= r0 && s_row[tid + 32] < r0 + BAND_M;
+            const unsigned b0 = __ballot_sync(FULL, in0), b1 = __ballot_sync(FULL, in1);
+            if (tid == 0) { s_mask[0] = b0; s_mask[1] = b1; }
+        }
+        __syncthreads();
+        if (PIPE) {
+            const T *tA = sAcc + buf * BAND_M * BAND_N;
+#pragma unroll
+            for (int b = 0; b < BAND_TN; b++)
+#pragma unroll
+                for (int a = 0; a < BAND_TM; a++)
+                    acc[a][b] = tA[(tc * BAND_TN + b) * BAND_M + tr * BAND_TM + a];
+        }
+        unsigned mk0 = s_mask[0], mk1 = s_mask[1];
+        while (mk0 | mk1) {                           // those rows take an original top row
+            int e;
+            if (mk0) { e = __ffs(mk0) - 1; mk0 &= mk0 - 1; }
+            else     { e = 32 + __ffs(mk1) - 1; mk1 &= mk1 - 1; }
+            const int lr = s_row[e] - r0 - tr * BAND_TM, top = s_src[e] - j0;
+            if (lr >= 0 && lr < BAND_TM && top >= 0 && top < PANEL_NB) {
+#pragma unroll
+                for (int a = 0; a < BAND_TM; a++)
+                    if (lr == a)
+#pragma unroll
+                        for (int b = 0; b < BAND_TN; b++)
+                            acc[a][b] = sTop[top * BAND_TOP_LD + tc * BAND_TN + b];
+            }
+        }
+        int k = 0;
+        for (; k + 4 <= ib; k += 4) {
+            T uu[BAND_TN][4];
+#pragma unroll
+            for (int b = 0; b < BAND_TN; b++)
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++) uu[b][kk] = sU[(tc * BAND_TN + b) * GEMM_LDU + k + kk];
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++) {
+                T l[BAND_TM];
+#pragma unroll
+                for (int a = 0; a < BAND_TM; a++) l[a] = tL[(k + kk) * BAND_M + tr * BAND_TM + a];
+#pragma unroll
+                for (int a = 0; a < BAND_TM; a++)
+#pragma unroll
+                    for (int b = 0; b < BAND_TN; b++)
+                        acc[a][b] = Prec<T>::fma_(-l[a], uu[b][kk], acc[a][b]);
+            }
+        }
+        for (; k < ib; k++) {
+            T l[BAND_TM], uu[BAND_TN];
+#pragma unroll
+            for (int a = 0; a < BAND_TM; a++) l[a] = tL[k * BAND_M + tr * BAND_TM + a];
+#pragma unroll
+            for (int b = 0; b < BAND_TN; b++) uu[b] = sU[(tc * BAND_TN + b) * GEMM_LDU + k];
+#pragma unroll
+            for (int a = 0; a < BAND_TM; a++)
+#pragma unroll
+                for (int b = 0; b < BAND_TN; b++) acc[a][b] = Prec<T>::fma_(-l[a], uu[b], acc[a][b]);
+        }
+#pragma unroll
+        for (int b = 0; b < BAND_TN; b++) {
+            const int c = c0 + tc * BAND_TN + b;
+#pragma unroll
+            for (int a = 0; a < BAND_TM; a++) {
+                const int r = r0 + tr * BAND_TM + a;
+                if (r < m && c < n) A[r + (size_t)c * ld] = acc[a][b];
+            }
+        }
+        if (PIPE) __syncthreads();                    // buffer buf free for the copies after next
+    }
+    if (PIPE) cp_async_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
+// Interchanges of the later panels applied, after the last step, to the
+// columns of an earlier panel (LAPACK applies them step by step; the columns
+// left of the current panel are read by no step, so the order of these moves
+// relative to the steps does not matter).  One CTA per (matrix, panel): panel
+// [pj0, pj1) takes the interchanges k = pj1 .. mn-1, in that order, on rows
+// [pj1, m).  As a gather, new row i = old row tau(i) with
+// tau = P_pj1 o P_pj1+1 o ... o P_mn-1 (P_k the transposition (k, ipiv[k]-1)),
+// so each thread finds tau for its rows alone by running the transpositions
+// from the last to the first.  The columns then move through shared memory a
+// chunk at a time, coalesced both ways.  Rows per matrix: at most
+// LEFT_ROWS * LEFT_THREADS (2 or 4 rows per thread).
+constexpr int LEFT_THREADS = 256;
+constexpr int LEFT_DEFER_MAX_M = LEFT_THREADS * 4;
+constexpr size_t LEFT_BUF_BYTES = 24 * 1024;
+
+template <typename T, int LEFT_ROWS>
+__global__ void __launch_bounds__(LEFT_THREADS)
+left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ipiv_array,
+                  StepSizes vs)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sbuf = reinterpret_cast<T *>(smem_raw);        // [cols][seg]
+    __shared__ int s_piv[LEFT_DEFER_MAX_M];
+    __shared__ int s_pj[2];
+    const int mat = blockIdx.y, tid = threadIdx.x;
+    if (tid == 0) {                                   // the panel's columns, as the steps chose them
+        int j = 0;
+        for (int b = 0; b < (int)blockIdx.x; b++) j += blocked_panel_width<T>(gm, gn, j);
+        s_pj[0] = j;
+        s_pj[1] = j + blocked_panel_width<T>(gm, gn, j);
+    }
+    __syncthreads();
+    const int pj0 = s_pj[0], pj1 = s_pj[1];
+    int ib = pj1 - pj0;
+    if (!vs.get(mat, pj0, m, n, ldda, ib)) return;
+    const int mn = min(m, n);
+    if (pj1 >= mn) return;                            // the matrix's last panel: nothing later
+    T *A = dA_array[mat];
+    const int *ipiv = ipiv_array[mat];
+    const int seg = m - pj1, nk = mn - pj1;
+    for (int k = tid; k < nk; k += LEFT_THREADS) s_piv[k] = ipiv[pj1 + k] - 1;
+    __syncthreads();
+    int tau[LEFT_ROWS];
+#pragma unroll
+    for (int u = 0; u < LEFT_ROWS; u++) tau[u] = pj1 + tid + u * LEFT_THREADS;
+    for (int k = mn - 1; k >= pj1; k--) {
+        const int p = s_piv[k - pj1];
+#pragma unroll
+        for (int u = 0; u < LEFT_ROWS; u++) tau[u] = tau[u] == k ? p : (tau[u] == p ? k : tau[u]);
+    }
+    const int cols = max(1, min(ib, (int)(LEFT_BUF_BYTES / ((size_t)seg * sizeof(T)))));
+    for (int cb = pj0; cb < pj0 + ib; cb += cols) {
+        const int wc = min(cols, pj0 + ib - cb);
+        const int total = wc * seg;
+        for (int e0 = tid; e0 < total; e0 += 8 * LEFT_THREADS) {
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int e = e0 + u * LEFT_THREADS;
+                if (e < total) v[u] = A[pj1 + e % seg + (size_t)(cb + e / seg) * ldda];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int e = e0 + u * LEFT_THREADS;
+                if (e < total) sbuf[e] = v[u];        // [c][i]
+            }
+        }
+        __syncthreads();
+        for (int c = 0; c < wc; c++) {
+#pragma unroll
+            for (int u = 0; u < LEFT_ROWS; u++) {
+                const int i = pj1 + tid + u * LEFT_THREADS, src = tau[u] - pj1;
+                if (i < m && tau[u] != i && src >= 0 && src < seg)
+                    A[i + (size_t)(cb + c) * ldda] = sbuf[c * seg + src];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+constexpr size_t left_swaps_smem_bytes() { return LEFT_BUF_BYTES; }
+
 // Panel width of the step at column j0 (32, halved while the panel's shared
 // memory copy does not fit).
 template <typename T>
-int blocked_panel_width(int m, int n, int j0)
+__host__ __device__ int blocked_panel_width(int m, int n, int j0)
 {
     const int want = min(PANEL_NB, min(m, n) - j0);
     if (panel_rows_per_thread<T>(m - j0) > 0) return want;
@@ -193,13 +572,33 @@ static void launch_panel(int rpt, int m, int n, int j0, int ib, T **dA, int ldda
             m, n, j0, ib, dA, ldda, ipiv, info, vs));
 }
 
+static int mlu_sm_count()
+{
+    static int count = 0;
+    if (!count) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            count <= 0) {
+            cudaGetLastError();
+            count = 1;
+        }
+    }
+    return count;
+}
+
 // One step of the blocked factorisation for every matrix: panel at column j0
 // of width ib, interchanges + TRSM, and (when `update`) the trailing update.
+// Right of the panel, band_kernel does all three in one launch (FP32, when the
+// batch gives it at least two CTAs per SM); otherwise swap_trsm_kernel and
+// gemm_kernel (more, smaller CTAs) do.  `defer_left`: the interchanges left of
+// the panel are left to left_swaps_kernel after the last step.
 // `vsz`: per-matrix sizes of a variable-size batch (m, n = their maxima).
 template <typename T>
 magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, int *info, int batch,
                                   magma_queue_t q, int j0, int ib, bool update,
-                                  StepSizes vsz = {nullptr, nullptr, nullptr})
+                                  StepSizes vsz = {nullptr, nullptr, nullptr},
+                                  bool defer_left = false)
 {
     cudaStream_t s = q->stream;
     constexpr int BM = 64, BN = 64, TM = 4, TN = 4;
@@ -213,6 +612,7 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
         mlu_allow_dynamic_smem(panel_regs_kernel<T, 1, true>);
         mlu_allow_dynamic_smem(panel_regs_kernel<T, 2, true>);
         mlu_allow_dynamic_smem(panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2), true>);
+        mlu_allow_dynamic_smem(band_kernel<T>);
     }
     const int pm = m - j0;
     const int rpt = panel_rows_per_thread<T>(pm);
@@ -240,13 +640,20 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
             launch_panel<T, true>(rpt, m, n, j0, ib, dAb, ldda, nullptr, infb, vs, nb, smem, s);
         else
             launch_panel<T, false>(rpt, m, n, j0, ib, dAb, ldda, ipb, infb, vs, nb, smem, s);
-        const int ncl = (j0 + SWAP_COLS - 1) / SWAP_COLS;
-        const int ncr = (n - j0 - ib + SWAP_COLS - 1) / SWAP_COLS;
+        const int rm = m - j0 - ib, rn = n - j0 - ib;
+        const int bands = rn > 0 ? (rn + BAND_N - 1) / BAND_N : 0;
+        const bool fused = band_used<T>() && update && bands > 0 &&
+                           (long long)bands * nb >= 2LL * mlu_sm_count();
+        const int ncl = defer_left ? 0 : (j0 + SWAP_COLS - 1) / SWAP_COLS;
+        const int ncr = fused ? 0 : (rn + SWAP_COLS - 1) / SWAP_COLS;
         if (ncl + ncr > 0)
             MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, swap_trsm_kernel<T><<<dim3(ncl + ncr, nb), SWAP_THREADS, 0, s>>>(
+                m, n, j0, ib, dAb, ldda, ipb, vs, defer_left ? 0 : 1));
+        if (fused) {
+            MLU_LAUNCH(mlu::KC_GEMM, s, band_kernel<T><<<dim3(bands, nb), BAND_THREADS,
+                                                         band_smem_bytes<T>(), s>>>(
                 m, n, j0, ib, dAb, ldda, ipb, vs));
-        const int rm = m - j0 - ib, rn = n - j0 - ib;
-        if (update && rm > 0 && rn > 0) {
+        } else if (update && rm > 0 && rn > 0) {
             const int tiles_m = (rm + BM - 1) / BM, tiles_n = (rn + BN - 1) / BN;
             MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
                                                                             (BM / TM) * (BN / TN), 0, s>>>(
@@ -264,19 +671,53 @@ magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int 
     return blocked_getrf_steps_l<T>(m, n, dA, ldda, ipiv, info, batch, q, j0, ib, update);
 }
 
+// The deferred interchanges left of each panel (left_swaps_kernel), for the
+// `panels` panels the steps over max sizes (gm, gn) made.
+template <typename T>
+static magma_int_t launch_left_swaps(int m, int n, int gm, int gn, T **dA, int ldda, int **ipiv,
+                                     int batch, int panels, StepSizes vsz, cudaStream_t s)
+{
+    if (panels < 2) return MAGMA_SUCCESS;
+    for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
+        const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
+        StepSizes vs = vsz;
+        if (vs.m_arr) {
+            vs.m_arr += b0;
+            vs.n_arr += b0;
+            vs.ld_arr += b0;
+        }
+        if (gm <= 2 * LEFT_THREADS)
+            MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, left_swaps_kernel<T, 2><<<dim3(panels - 1, nb), LEFT_THREADS,
+                                                                       left_swaps_smem_bytes<T>(), s>>>(
+                m, n, gm, gn, dA + b0, ldda, ipiv + b0, vs));
+        else
+            MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, left_swaps_kernel<T, 4><<<dim3(panels - 1, nb), LEFT_THREADS,
+                                                                       left_swaps_smem_bytes<T>(), s>>>(
+                m, n, gm, gn, dA + b0, ldda, ipiv + b0, vs));
+    }
+    MLU_CHECK_LAUNCH();
+    return MAGMA_SUCCESS;
+}
+
 template <typename T>
 magma_int_t blocked_getrf(int m, int n, T **dA, int ldda, int **ipiv, int *info, int batch,
                           magma_queue_t q)
 {
     if (batch <= 0 || m == 0 || n == 0) return MAGMA_SUCCESS;
     const int mn = min(m, n);
-    for (int j0 = 0; j0 < mn;) {
+    const bool defer = ipiv != nullptr && m <= LEFT_DEFER_MAX_M;
+    int panels = 0;
+    for (int j0 = 0; j0 < mn; panels++) {
         const int ib = blocked_panel_width<T>(m, n, j0);
         const magma_int_t rc = blocked_getrf_steps_l<T>(m, n, dA, ldda, ipiv, info, batch, q, j0,
-                                                        ib, true);
+                                                        ib, true, {nullptr, nullptr, nullptr},
+                                                        defer);
         if (rc != 0) return rc;
         j0 += ib;
     }
+    if (defer)
+        return launch_left_swaps<T>(m, n, m, n, dA, ldda, ipiv, batch, panels,
+                                    {nullptr, nullptr, nullptr}, q->stream);
     return MAGMA_SUCCESS;
 }
 
@@ -297,13 +738,18 @@ magma_int_t blocked_getrf_vbatched(const int *m, const int *n, const int *ld, in
     if (batch <= 0 || max_m <= 0 || max_n <= 0) return MAGMA_SUCCESS;
     const int mn = min(max_m, max_n);
     const StepSizes vs = {m, n, ld};
-    for (int j0 = 0; j0 < mn;) {
+    const bool defer = ipiv != nullptr && max_m <= LEFT_DEFER_MAX_M;
+    int panels = 0;
+    for (int j0 = 0; j0 < mn; panels++) {
         const int ib = blocked_panel_width<T>(max_m, max_n, j0);
         const magma_int_t rc = blocked_getrf_steps_l<T>(max_m, max_n, dA, 0, ipiv, info, batch, q,
-                                                        j0, ib, true, vs);
+                                                        j0, ib, true, vs, defer);
         if (rc != 0) return rc;
         j0 += ib;
     }
+    if (defer)
+        return launch_left_swaps<T>(max_m, max_n, max_m, max_n, dA, 0, ipiv, batch, panels, vs,
+                                    q->stream);
     return MAGMA_SUCCESS;
 }
 template magma_int_t blocked_getrf_vbatched<double>(const int *, const int *, const int *, int, int,

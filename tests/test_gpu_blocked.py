@@ -126,3 +126,53 @@ def test_gesv_n1024_fp64(cuda):
     assert np.array_equal(ipiv.cpu().numpy(), ripiv)
     assert np.array_equal(dX.cpu().numpy(), rX)
     assert np.array_equal(dS.cpu().numpy(), rS)
+
+
+# Batches large enough for the fused band kernel (interchanges + TRSM + trailing
+# update in one launch per step, at least two CTAs per SM): square, tall, wide
+# (steps with no rows below the panel), padded ld with singular columns, FP32
+# register panels of four rows per thread, m above the deferred-interchange
+# limit, and steps that switch between the band kernel and the per-tile kernels
+# as the bands run out.
+@pytest.mark.parametrize("m,n,batch,dtype", [(100, 100, 320, np.float64),
+                                             (100, 100, 320, np.float32),
+                                             (300, 200, 160, np.float64),
+                                             (150, 400, 160, np.float64),
+                                             (520, 520, 48, np.float32),
+                                             (1100, 64, 320, np.float64)])
+def test_getrf_band_path_bitexact(cuda, m, n, batch, dtype):
+    rng = np.random.default_rng(m + 7 * n + batch)
+    S = to_storage(rng.uniform(-1, 1, (batch, m, n)).astype(dtype))
+    rS = S.copy()
+    f = oracle.dgetrf_batched if dtype == np.float64 else oracle.sgetrf_batched
+    ripiv, rinfo = f(rS, m)
+    gS, gipiv, ginfo = _gpu_getrf(S, m, cuda)
+    k = min(m, n)
+    assert np.array_equal(ginfo, rinfo)
+    assert np.array_equal(gipiv[:, :k], ripiv[:, :k])
+    assert np.array_equal(gS, rS)
+
+
+def test_band_path_padded_ld_singular_and_solve(cuda):
+    rng = np.random.default_rng(91)
+    n, ld, batch = 90, 128, 320
+    A = rng.uniform(-1, 1, (batch, n, n))
+    A[1, :, 3] = 0.0
+    A[2] = 0.0
+    A[3, :, 89] = 0.0
+    Bm = rng.uniform(-1, 1, (batch, n, 2))
+    S, X = to_storage(A, ld), to_storage(Bm, ld)
+    S[:, :, n:] = 5.0
+    rS, rX = S.copy(), X.copy()
+    ripiv, rinfo = oracle.dgesv_batched(rS, rX)
+    dS, dX = torch.from_numpy(S).to(cuda), torch.from_numpy(X).to(cuda)
+    ipiv, info = mg.gesv_batched(dS, dX)
+    torch.cuda.synchronize()
+    ginfo = info.cpu().numpy()
+    assert np.array_equal(ginfo, rinfo)
+    assert list(ginfo[:4]) == [0, 4, 1, 90]
+    assert np.array_equal(ipiv.cpu().numpy(), ripiv)
+    assert np.array_equal(dS.cpu().numpy(), rS)
+    good = ginfo == 0
+    assert np.array_equal(dX.cpu().numpy()[good], rX[good])
+    assert np.all(dS.cpu().numpy()[:, :, n:] == 5.0)
