@@ -168,20 +168,27 @@ gemm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int tiles_m, S
 }
 
 // ---------------------------------------------------------------------------
-// The step right of the panel in one launch: one CTA per (matrix, BAND_N-column
-// band of columns j0+ib..n).
-//   1. the step's interchanges as a table of touched rows (build_permutation);
+// FP32: the step right of the panel in one launch, one CTA per (matrix,
+// BAND_N-column band of columns j0+ib..n).
+//   1. the step's interchanges as a table of touched rows (build_permutation,
+//      warp 0, while the other loads are in flight);
 //   2. the band's original top rows (rows j0..j0+ib) and L11 staged in shared
 //      memory, coalesced;
 //   3. the interchanged top rows, i.e. U12 before the solve: a top row's new
 //      content is an original top row (from shared memory) or a row further
 //      down (the only scattered reads: at most ib rows of the band);
-//   4. U12 = L11^{-1} U12 in registers, one thread per column, written back;
-//   5. every BAND_M-row tile below: A22 -= L21 U12 with U12 from shared
-//      memory.  A row that receives an original top row in this step's
-//      interchanges (always a top row: each interchange k moves row j0+k, which
-//      still holds an original top row, down) takes its value from shared
-//      memory, so the interchanges need no scattered writes.
+//   4. U12 = L11^{-1} U12 in registers, one thread per column, kept in shared
+//      memory (k-major) and written back;
+//   5. A22 -= L21 U12 in strips of 64 rows x 32 columns, one warp per strip and
+//      no block-wide barrier: lane l owns rows l and l+32 of the strip, so
+//      every global load and store of A22 is a coalesced 128-byte row segment;
+//      the warp stages its strip of L21 in its own shared memory (cp.async),
+//      and per k a lane reads its two L21 values (one 8-byte load) and the
+//      strip's 32 U12 values (eight broadcast 16-byte loads) for 64 FMAs.  A
+//      row that receives an original top row in this step's interchanges
+//      (always a top row: each interchange k moves row j0+k, which still holds
+//      an original top row, down) takes its value from shared memory, so the
+//      interchanges need no scattered writes.
 // Per element the same operations, in the same order, as swap_trsm_kernel
 // followed by gemm_kernel.  Columns left of the panel are not touched (their
 // interchanges are applied by swap_trsm_kernel or, after the last step, by
@@ -189,34 +196,28 @@ gemm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int tiles_m, S
 template <typename T>
 __host__ __device__ int blocked_panel_width(int m, int n, int j0);
 
-constexpr int BAND_N = 64, BAND_M = 64, BAND_TM = 4, BAND_TN = 4;
-constexpr int BAND_THREADS = (BAND_M / BAND_TM) * (BAND_N / BAND_TN);
-constexpr int BAND_TOP_LD = BAND_N + 1;
+constexpr int BAND_N = 64;                            // columns per band (per CTA)
+constexpr int BAND_THREADS = 256;
+constexpr int BAND_WARPS = BAND_THREADS / 32;
+constexpr int STRIP_M = 64, STRIP_N = 32;             // one warp's piece of A22
+constexpr int BAND_TOP_LD = BAND_N + 1;               // original top rows [k][j]
+constexpr int BAND_U_LD = BAND_N + 4;                 // U12 [k][j], 16-byte rows
 constexpr int BAND_LOADS = PANEL_NB * BAND_N / BAND_THREADS;   // per thread, 8
-static_assert(BAND_M == BAND_N && BAND_LOADS * BAND_THREADS == PANEL_NB * BAND_N, "band tiling");
+static_assert(BAND_LOADS * BAND_THREADS == PANEL_NB * BAND_N, "band staging");
+static_assert(STRIP_M == 64 && STRIP_N == 32 && BAND_N == 2 * STRIP_N, "strip layout");
 
-// The band kernel is used for FP32 only.  In FP64 its one-warp-pair TRSM
-// prologue runs on the FP64 pipe while the CTA's other warps wait, and the
-// separate interchange/TRSM and update kernels were faster on GB300 (79.4 ms
-// against 85.6 ms for the variable-size FP64 solve of 256 matrices of order
-// 128..1024; 10.44 ms against 10.76 ms for the FP32 factorisation of 512
-// matrices of order 512 inside the refinement).
+// The band kernel is used for FP32 only.  An FP64 version (one thread per
+// column for the solve, 4x4 tiles) was slower than the separate interchange/TRSM
+// and update kernels on GB300 (85.6 ms against 79.4 ms for the variable-size
+// FP64 solve of 256 matrices of order 128..1024): its solve prologue runs on
+// the FP64 pipe while the CTA's other warps wait.
 template <typename T>
 __host__ __device__ constexpr bool band_used() { return sizeof(T) == 4; }
 
-// FP32: the tiles' A22 and L21 blocks are double-buffered in shared memory
-// (cp.async), so a tile's loads overlap the previous tile's FMAs.  FP64 keeps
-// one L21 buffer and loads A22 into registers (its FMA rate, not latency,
-// bounds it, and the buffers would leave one CTA per SM).
-template <typename T>
-__host__ __device__ constexpr bool band_pipelined() { return sizeof(T) == 4; }
-
-template <typename T>
 __host__ __device__ constexpr size_t band_smem_bytes()
 {
-    return sizeof(T) * ((size_t)BAND_N * GEMM_LDU + (size_t)PANEL_NB * BAND_TOP_LD +
-                        (band_pipelined<T>() ? 2 * ((size_t)PANEL_NB * BAND_M + (size_t)BAND_M * BAND_N)
-                                             : (size_t)PANEL_NB * BAND_M));
+    return sizeof(float) * ((size_t)PANEL_NB * BAND_U_LD + 2 * (size_t)PANEL_NB * BAND_TOP_LD +
+                            (size_t)PANEL_NB * (PANEL_NB + 1) + (size_t)BAND_WARPS * PANEL_NB * STRIP_M);
 }
 
 // cp.async of one element (4 or 8 bytes) to shared memory; `valid` false
@@ -233,56 +234,60 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-template <typename T>
-__global__ void __launch_bounds__(BAND_THREADS, sizeof(T) == 4 ? 3 : 2)
-band_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array, StepSizes vs)
+__global__ void __launch_bounds__(BAND_THREADS, 2)
+band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv_array, StepSizes vs)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr bool PIPE = band_pipelined<T>();
-    T *sU = reinterpret_cast<T *>(smem_raw);          // [BAND_N][GEMM_LDU]: U12, transposed
-    T *sTop = sU + BAND_N * GEMM_LDU;                 // [PANEL_NB][BAND_TOP_LD]: original top rows
-    T *sL = sTop + PANEL_NB * BAND_TOP_LD;            // [2][PANEL_NB][BAND_M]: L21 tiles (L11 first)
-    T *sAcc = sL + (PIPE ? 2 : 1) * PANEL_NB * BAND_M;   // [2][BAND_N][BAND_M]: A22 tiles (PIPE)
-    __shared__ int s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt, s_top_src[PANEL_NB];
-    __shared__ unsigned s_mask[2];
-    const int mat = blockIdx.y, tid = threadIdx.x;
+    float *sU = reinterpret_cast<float *>(smem_raw);  // [PANEL_NB][BAND_U_LD]: U12, k-major
+    float *sTop = sU + PANEL_NB * BAND_U_LD;          // [PANEL_NB][BAND_TOP_LD]: original top rows
+    float *sP = sTop + PANEL_NB * BAND_TOP_LD;        // [PANEL_NB][BAND_TOP_LD]: pivot rows below
+    float *sL11 = sP + PANEL_NB * BAND_TOP_LD;        // [PANEL_NB][PANEL_NB+1]
+    float *sLw = sL11 + PANEL_NB * (PANEL_NB + 1);    // [warp][k][64 rows]: L21 strips
+    __shared__ int s_p[PANEL_NB], s_top_src[PANEL_NB], s_top_idx[PANEL_NB];
+    __shared__ int s_row[PANEL_NB], s_src[PANEL_NB];
+    const int mat = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (!vs.get(mat, j0, m, n, ldda, ib)) return;
     const int c0 = j0 + ib + blockIdx.x * BAND_N;
     if (c0 >= n) return;                              // past this matrix's columns
     const int w = min(BAND_N, n - c0);
-    T *A = dA_array[mat];
+    float *A = dA_array[mat];
     const size_t ld = ldda;
+    const int r_first = j0 + ib;
+    const int strips_r = m > r_first ? (m - r_first + STRIP_M - 1) / STRIP_M : 0;
+    const int halves = (w + STRIP_N - 1) / STRIP_N;
+    const int nstrips = strips_r * halves;
+    float *myL = sLw + warp * PANEL_NB * STRIP_M;     // [k][lane*2 + h]
+    // strip sidx's L21 rows (lane, lane+32) into this warp's buffer
+    auto issue_L = [&](int sidx) {
+        const int ra = r_first + (sidx / halves) * STRIP_M + lane, rb = ra + 32;
+#pragma unroll 4
+        for (int k = 0; k < PANEL_NB; k++) {
+            const bool ka = k < ib;
+            cp_async_elem<4>(myL + k * STRIP_M + lane * 2, ka && ra < m ? A + ra + (size_t)(j0 + k) * ld : A,
+                             ka && ra < m);
+            cp_async_elem<4>(myL + k * STRIP_M + lane * 2 + 1,
+                             ka && rb < m ? A + rb + (size_t)(j0 + k) * ld : A, ka && rb < m);
+        }
+        cp_async_commit();
+    };
+    // L21 is final (the panel kernel wrote it): the first strips' copies go first
+    if (warp < nstrips) issue_L(warp);
+    // pivot targets, the band's original top rows and L11, all in flight together
+    int p = j0 + lane;
+    if (warp == 0 && ipiv_array != nullptr && lane < ib) p = ipiv_array[mat][j0 + lane] - 1;
     {
-        // original top rows of the band and L11: all loads in flight while warp 0
-        // builds the interchange table
-        T v[BAND_LOADS], l[PANEL_NB * PANEL_NB / BAND_THREADS];
+        float v[BAND_LOADS], l[PANEL_NB * PANEL_NB / BAND_THREADS];
 #pragma unroll
         for (int u = 0; u < BAND_LOADS; u++) {
             const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
-            v[u] = (k < ib && j < w) ? A[j0 + k + (size_t)(c0 + j) * ld] : T(0);
+            v[u] = (k < ib && j < w) ? A[j0 + k + (size_t)(c0 + j) * ld] : 0.f;
         }
 #pragma unroll
         for (int u = 0; u < PANEL_NB * PANEL_NB / BAND_THREADS; u++) {
             const int e = tid + u * BAND_THREADS, i = e % PANEL_NB, t = e / PANEL_NB;
-            l[u] = (i < ib && t < ib) ? A[j0 + i + (size_t)(j0 + t) * ld] : T(0);
+            l[u] = (i < ib && t < ib) ? A[j0 + i + (size_t)(j0 + t) * ld] : 0.f;
         }
-        if (tid < 32) {
-            if (ipiv_array == nullptr) {              // no pivoting: no interchanges
-                if (tid == 0) s_cnt = 0;
-            } else {
-                build_permutation(ipiv_array[mat], j0, ib, s_row, s_src, &s_cnt);
-            }
-            // where each top row's new content comes from (identity, then the
-            // table's entries inside the top block)
-            s_top_src[tid] = j0 + tid;
-            __syncwarp();
-            const int cnt = ipiv_array == nullptr ? 0 : s_cnt;
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int e = tid + 32 * h;
-                if (e < cnt && s_row[e] < j0 + ib) s_top_src[s_row[e] - j0] = s_src[e];
-            }
-        }
+        if (warp == 0) s_p[lane] = p;
 #pragma unroll
         for (int u = 0; u < BAND_LOADS; u++) {
             const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
@@ -291,171 +296,151 @@ band_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_arr
 #pragma unroll
         for (int u = 0; u < PANEL_NB * PANEL_NB / BAND_THREADS; u++) {
             const int e = tid + u * BAND_THREADS, i = e % PANEL_NB, t = e / PANEL_NB;
-            sL[i * (PANEL_NB + 1) + t] = l[u];         // L11[i][t]
+            sL11[i * (PANEL_NB + 1) + t] = l[u];       // L11[i][t]
         }
     }
     __syncthreads();
     {
-        T v[BAND_LOADS];
+        // the band's segments of the pivot rows below the top block (the only
+        // rows below that can move up), while warp 0 resolves the interchanges
+        float v[BAND_LOADS];
 #pragma unroll
         for (int u = 0; u < BAND_LOADS; u++) {
-            const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
-            v[u] = T(0);
-            if (k < ib && j < w) {
-                const int src = s_top_src[k];
-                v[u] = src < j0 + ib ? sTop[(src - j0) * BAND_TOP_LD + j]
-                                     : A[src + (size_t)(c0 + j) * ld];
+            const int e = tid + u * BAND_THREADS, j = e % BAND_N, k = e / BAND_N;
+            const int pk = s_p[k];
+            v[u] = (k < ib && pk >= r_first && j < w) ? A[pk + (size_t)(c0 + j) * ld] : 0.f;
+        }
+        if (warp == 0) {
+            // The step's interchanges k = 0..ib-1 exchange rows j0+k and p_k in
+            // turn; as a gather, new row x = old row tau(x) with
+            // tau = P_0 o P_1 o ... o P_ib-1, found by applying the
+            // transpositions from the last to the first.  Lane k resolves top
+            // row j0+k and pivot row p_k; idx remembers which pivot row (if
+            // any) a value is.
+            int vt = j0 + lane, it = -1, vp = p, ip = lane;
+            for (int k = ib - 1; k >= 0; k--) {
+                const int a = j0 + k, pk = __shfl_sync(FULL, p, k);
+                if (vt == a) { vt = pk; it = k; } else if (vt == pk) { vt = a; it = -1; }
+                if (vp == a) { vp = pk; ip = k; } else if (vp == pk) { vp = a; ip = -1; }
             }
+            s_top_src[lane] = vt;
+            s_top_idx[lane] = it;
+            // a pivot row below the top block always ends up holding an
+            // original top row (interchange k moves row j0+k, which still
+            // holds an original top row, down)
+            s_row[lane] = (lane < ib && p >= r_first) ? p : -1;
+            s_src[lane] = vp;
         }
 #pragma unroll
         for (int u = 0; u < BAND_LOADS; u++) {
-            const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
-            sU[j * GEMM_LDU + k] = v[u];
+            const int e = tid + u * BAND_THREADS, j = e % BAND_N, k = e / BAND_N;
+            sP[k * BAND_TOP_LD + j] = v[u];
         }
     }
     __syncthreads();
-    if (tid < w) {                                    // U12 = L11^{-1} U12, column tid
-        T x[PANEL_NB];
+    // interchanged top rows into sU[k][j]
 #pragma unroll
-        for (int k = 0; k < PANEL_NB; k++) x[k] = sU[tid * GEMM_LDU + k];
+    for (int u = 0; u < BAND_LOADS; u++) {
+        const int e = tid + u * BAND_THREADS, j = e % BAND_N, k = e / BAND_N;
+        float x = 0.f;
+        if (k < ib) {
+            const int src = s_top_src[k], idx = s_top_idx[k];
+            if (src < r_first) x = sTop[(src - j0) * BAND_TOP_LD + j];
+            else if (idx >= 0) x = sP[idx * BAND_TOP_LD + j];
+        }
+        sU[k * BAND_U_LD + j] = x;
+    }
+    __syncthreads();
+    {
+        // U12 = L11^{-1} U12: four lanes per column, lane q of a group owns rows
+        // 8q..8q+7; x_t comes from its owner by a shuffle, then
+        // x_i = fma(-l_it, x_t, x_i) for i > t, t ascending
+        const int col = tid >> 2, q = tid & 3;
+        float x[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) x[r] = sU[(q * 8 + r) * BAND_U_LD + col];
 #pragma unroll
         for (int t = 0; t < PANEL_NB; t++) {
             if (t < ib) {
+                const float xt = __shfl_sync(FULL, x[t % 8], t / 8, 4);
 #pragma unroll
-                for (int i = t + 1; i < PANEL_NB; i++)
-                    if (i < ib) x[i] = Prec<T>::fma_(-sL[i * (PANEL_NB + 1) + t], x[t], x[i]);
+                for (int r = 0; r < 8; r++) {
+                    const int i = q * 8 + r;
+                    if (i > t && i < ib) x[r] = fmaf(-sL11[i * (PANEL_NB + 1) + t], xt, x[r]);
+                }
             }
         }
 #pragma unroll
-        for (int k = 0; k < PANEL_NB; k++) sU[tid * GEMM_LDU + k] = x[k];
+        for (int r = 0; r < 8; r++) sU[(q * 8 + r) * BAND_U_LD + col] = x[r];
     }
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < BAND_LOADS; u++) {
         const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
-        if (k < ib && j < w) A[j0 + k + (size_t)(c0 + j) * ld] = sU[j * GEMM_LDU + k];
+        if (k < ib && j < w) A[j0 + k + (size_t)(c0 + j) * ld] = sU[k * BAND_U_LD + j];
     }
-    const int tr = tid % (BAND_M / BAND_TM), tc = tid / (BAND_M / BAND_TM);
-    // copies of tile r0's A22 block ([c][r]) and L21 block ([k][r]) into buffer buf
-    auto issue = [&](int r0, int buf) {
-        T *dAcc = sAcc + buf * BAND_M * BAND_N, *dL = sL + buf * PANEL_NB * BAND_M;
+    // strips of A22, one warp each
+    for (int sidx = warp; sidx < nstrips; sidx += BAND_WARPS) {
+        if (sidx != warp) issue_L(sidx);
+        const int r0 = r_first + (sidx / halves) * STRIP_M;
+        const int cs = (sidx % halves) * STRIP_N;     // first column of the strip in the band
+        const int ra = r0 + lane, rb = r0 + lane + 32;
+        float acc0[STRIP_N], acc1[STRIP_N];
 #pragma unroll
-        for (int u = 0; u < BAND_M * BAND_N / BAND_THREADS; u++) {
-            const int e = tid + u * BAND_THREADS, r = e % BAND_M, c = e / BAND_M;
-            const bool ok = r0 + r < m && c < w;
-            cp_async_elem<sizeof(T)>(dAcc + e, ok ? A + r0 + r + (size_t)(c0 + c) * ld : A, ok);
+        for (int c = 0; c < STRIP_N; c++) {
+            const bool cv = cs + c < w;
+            const float *colp = A + (size_t)(c0 + cs + c) * ld;
+            acc0[c] = (cv && ra < m) ? colp[ra] : 0.f;
+            acc1[c] = (cv && rb < m) ? colp[rb] : 0.f;
         }
+        // rows of this strip that receive an original top row
+        const int prow = s_row[lane];
+        unsigned mk = __ballot_sync(FULL, prow >= r0 && prow < r0 + STRIP_M);
+        while (mk) {
+            const int e = __ffs(mk) - 1;
+            mk &= mk - 1;
+            const int row = s_row[e], top = s_src[e] - j0;
+            if (top >= 0 && top < PANEL_NB) {
+                const float *srow = sTop + top * BAND_TOP_LD + cs;
+                if (row == ra) {
 #pragma unroll
-        for (int u = 0; u < BAND_LOADS; u++) {
-            const int e = tid + u * BAND_THREADS, i = e % BAND_M, kl = e / BAND_M;
-            const bool ok = kl < ib && r0 + i < m;
-            cp_async_elem<sizeof(T)>(dL + e, ok ? A + r0 + i + (size_t)(j0 + kl) * ld : A, ok);
-        }
-    };
-    __syncthreads();                                  // L11 no longer needed in sL
-    if (PIPE && j0 + ib < m) issue(j0 + ib, 0);
-    if (PIPE) cp_async_commit();
-    int buf = 0;
-    for (int r0 = j0 + ib; r0 < m; r0 += BAND_M, buf ^= 1) {
-        T acc[BAND_TM][BAND_TN];
-        const T *tL = sL + (PIPE ? buf * PANEL_NB * BAND_M : 0);
-        if (PIPE) {
-            if (r0 + BAND_M < m) issue(r0 + BAND_M, buf ^ 1);
-            cp_async_commit();
-            cp_async_wait<1>();                       // this tile's copies have landed
-        } else {
-            __syncthreads();                          // sL free again
+                    for (int c = 0; c < STRIP_N; c++) acc0[c] = srow[c];
+                } else if (row == rb) {
 #pragma unroll
-            for (int b = 0; b < BAND_TN; b++) {
-                const int c = c0 + tc * BAND_TN + b;
-#pragma unroll
-                for (int a = 0; a < BAND_TM; a++) {
-                    const int r = r0 + tr * BAND_TM + a;
-                    acc[a][b] = (r < m && c < n) ? A[r + (size_t)c * ld] : T(0);
+                    for (int c = 0; c < STRIP_N; c++) acc1[c] = srow[c];
                 }
             }
-            T vl[BAND_LOADS];
-#pragma unroll
-            for (int u = 0; u < BAND_LOADS; u++) {
-                const int e = tid + u * BAND_THREADS, i = e % BAND_M, kl = e / BAND_M;
-                vl[u] = (kl < ib && r0 + i < m) ? A[r0 + i + (size_t)(j0 + kl) * ld] : T(0);
-            }
-#pragma unroll
-            for (int u = 0; u < BAND_LOADS; u++) sL[tid + u * BAND_THREADS] = vl[u];
         }
-        if (tid < 32) {                               // touched rows inside this tile
-            const int cnt = s_cnt;
-            const bool in0 = tid < cnt && s_row[tid] >= r0 && s_row[tid] < r0 + BAND_M;
-            const bool in1 = tid + 32 < cnt && s_row[tid + 32] >= r0 && s_row[tid + 32] < r0 + BAND_M;
-            const unsigned b0 = __ballot_sync(FULL, in0), b1 = __ballot_sync(FULL, in1);
-            if (tid == 0) { s_mask[0] = b0; s_mask[1] = b1; }
-        }
-        __syncthreads();
-        if (PIPE) {
-            const T *tA = sAcc + buf * BAND_M * BAND_N;
+        cp_async_wait<0>();
+        __syncwarp();
+#pragma unroll 2
+        for (int k = 0; k < ib; k++) {
+            const float2 lv = *reinterpret_cast<const float2 *>(myL + k * STRIP_M + lane * 2);
+            const float4 *urow = reinterpret_cast<const float4 *>(sU + k * BAND_U_LD + cs);
 #pragma unroll
-            for (int b = 0; b < BAND_TN; b++)
-#pragma unroll
-                for (int a = 0; a < BAND_TM; a++)
-                    acc[a][b] = tA[(tc * BAND_TN + b) * BAND_M + tr * BAND_TM + a];
-        }
-        unsigned mk0 = s_mask[0], mk1 = s_mask[1];
-        while (mk0 | mk1) {                           // those rows take an original top row
-            int e;
-            if (mk0) { e = __ffs(mk0) - 1; mk0 &= mk0 - 1; }
-            else     { e = 32 + __ffs(mk1) - 1; mk1 &= mk1 - 1; }
-            const int lr = s_row[e] - r0 - tr * BAND_TM, top = s_src[e] - j0;
-            if (lr >= 0 && lr < BAND_TM && top >= 0 && top < PANEL_NB) {
-#pragma unroll
-                for (int a = 0; a < BAND_TM; a++)
-                    if (lr == a)
-#pragma unroll
-                        for (int b = 0; b < BAND_TN; b++)
-                            acc[a][b] = sTop[top * BAND_TOP_LD + tc * BAND_TN + b];
+            for (int qq = 0; qq < STRIP_N / 4; qq++) {
+                const float4 u4 = urow[qq];
+                acc0[4 * qq + 0] = fmaf(-lv.x, u4.x, acc0[4 * qq + 0]);
+                acc0[4 * qq + 1] = fmaf(-lv.x, u4.y, acc0[4 * qq + 1]);
+                acc0[4 * qq + 2] = fmaf(-lv.x, u4.z, acc0[4 * qq + 2]);
+                acc0[4 * qq + 3] = fmaf(-lv.x, u4.w, acc0[4 * qq + 3]);
+                acc1[4 * qq + 0] = fmaf(-lv.y, u4.x, acc1[4 * qq + 0]);
+                acc1[4 * qq + 1] = fmaf(-lv.y, u4.y, acc1[4 * qq + 1]);
+                acc1[4 * qq + 2] = fmaf(-lv.y, u4.z, acc1[4 * qq + 2]);
+                acc1[4 * qq + 3] = fmaf(-lv.y, u4.w, acc1[4 * qq + 3]);
             }
         }
-        int k = 0;
-        for (; k + 4 <= ib; k += 4) {
-            T uu[BAND_TN][4];
 #pragma unroll
-            for (int b = 0; b < BAND_TN; b++)
-#pragma unroll
-                for (int kk = 0; kk < 4; kk++) uu[b][kk] = sU[(tc * BAND_TN + b) * GEMM_LDU + k + kk];
-#pragma unroll
-            for (int kk = 0; kk < 4; kk++) {
-                T l[BAND_TM];
-#pragma unroll
-                for (int a = 0; a < BAND_TM; a++) l[a] = tL[(k + kk) * BAND_M + tr * BAND_TM + a];
-#pragma unroll
-                for (int a = 0; a < BAND_TM; a++)
-#pragma unroll
-                    for (int b = 0; b < BAND_TN; b++)
-                        acc[a][b] = Prec<T>::fma_(-l[a], uu[b][kk], acc[a][b]);
+        for (int c = 0; c < STRIP_N; c++) {
+            if (cs + c < w) {
+                float *colp = A + (size_t)(c0 + cs + c) * ld;
+                if (ra < m) colp[ra] = acc0[c];
+                if (rb < m) colp[rb] = acc1[c];
             }
         }
-        for (; k < ib; k++) {
-            T l[BAND_TM], uu[BAND_TN];
-#pragma unroll
-            for (int a = 0; a < BAND_TM; a++) l[a] = tL[k * BAND_M + tr * BAND_TM + a];
-#pragma unroll
-            for (int b = 0; b < BAND_TN; b++) uu[b] = sU[(tc * BAND_TN + b) * GEMM_LDU + k];
-#pragma unroll
-            for (int a = 0; a < BAND_TM; a++)
-#pragma unroll
-                for (int b = 0; b < BAND_TN; b++) acc[a][b] = Prec<T>::fma_(-l[a], uu[b], acc[a][b]);
-        }
-#pragma unroll
-        for (int b = 0; b < BAND_TN; b++) {
-            const int c = c0 + tc * BAND_TN + b;
-#pragma unroll
-            for (int a = 0; a < BAND_TM; a++) {
-                const int r = r0 + tr * BAND_TM + a;
-                if (r < m && c < n) A[r + (size_t)c * ld] = acc[a][b];
-            }
-        }
-        if (PIPE) __syncthreads();                    // buffer buf free for the copies after next
+        __syncwarp();                                 // the buffer is refilled for the next strip
     }
-    if (PIPE) cp_async_wait<0>();
+    cp_async_wait<0>();
 }
 
 // ---------------------------------------------------------------------------
@@ -612,7 +597,7 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
         mlu_allow_dynamic_smem(panel_regs_kernel<T, 1, true>);
         mlu_allow_dynamic_smem(panel_regs_kernel<T, 2, true>);
         mlu_allow_dynamic_smem(panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2), true>);
-        mlu_allow_dynamic_smem(band_kernel<T>);
+        if (band_used<T>()) mlu_allow_dynamic_smem(band_kernel);
     }
     const int pm = m - j0;
     const int rpt = panel_rows_per_thread<T>(pm);
@@ -650,9 +635,8 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
             MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, swap_trsm_kernel<T><<<dim3(ncl + ncr, nb), SWAP_THREADS, 0, s>>>(
                 m, n, j0, ib, dAb, ldda, ipb, vs, defer_left ? 0 : 1));
         if (fused) {
-            MLU_LAUNCH(mlu::KC_GEMM, s, band_kernel<T><<<dim3(bands, nb), BAND_THREADS,
-                                                         band_smem_bytes<T>(), s>>>(
-                m, n, j0, ib, dAb, ldda, ipb, vs));
+            MLU_LAUNCH(mlu::KC_GEMM, s, band_kernel<<<dim3(bands, nb), BAND_THREADS, band_smem_bytes(), s>>>(
+                m, n, j0, ib, reinterpret_cast<float **>(dAb), ldda, ipb, vs));
         } else if (update && rm > 0 && rn > 0) {
             const int tiles_m = (rm + BM - 1) / BM, tiles_n = (rn + BN - 1) / BN;
             MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
