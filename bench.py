@@ -198,6 +198,10 @@ class Dsgesv512:
     tol = 30.0
     itermax = 30
     precision = "fp32"
+    solver = "ir"
+    SOLVER = {"ir": "FP64 refinement",
+              "gmres": "FP64 refinement with each correction solved by FP32 GMRES preconditioned "
+                       "with the factors (Magma_REFINE_IRGMSTRS)"}
     FACTOR = {"fp32": "FP32 LU (SIMT FMA)",
               "fp16": "FP32 LU with FP16 tensor-core trailing updates (FP32 accumulation, "
                       "power-of-two row/column scaling)",
@@ -206,7 +210,8 @@ class Dsgesv512:
     def describe(self):
         return {"workload": "magma_dxgesv_batched_work: 512 FP64 matrices n=512, nrhs=4, "
                             "A=U diag(s) V^T, kappa in {1e2,1e4,1e6}; " + self.FACTOR[self.precision]
-                            + " + FP64 refinement, stop at scaled residual <= 30 or 30 iterations, "
+                            + " + " + self.SOLVER[self.solver]
+                            + f", stop at scaled residual <= 30 or {self.itermax} iterations, "
                             "FP64 re-solve of non-converged matrices",
                 "batch": self.batch, "n": self.n, "nrhs": self.nrhs,
                 "precision": f"{self.precision} factor, fp64 residual/update/convergence",
@@ -237,7 +242,8 @@ class Dsgesv512:
         c["ipiv"] = torch.empty((b, n), dtype=torch.int32, device=dev)
         c["info"] = torch.empty((b,), dtype=torch.int32, device=dev)
         c["iter"] = torch.empty((b,), dtype=torch.int32, device=dev)
-        c["work"] = torch.empty((mg.dsgesv_workspace_bytes(n, self.nrhs, b, self.precision),),
+        c["work"] = torch.empty((mg.dsgesv_workspace_bytes(n, self.nrhs, b, self.precision,
+                                                          self.solver),),
                                 dtype=torch.uint8, device=dev)
         c["lwork"] = C.c_size_t(c["work"].numel())
         for k in ("S", "B", "X", "ipiv"):
@@ -249,14 +255,15 @@ class Dsgesv512:
         return c
 
     def step(self, c, i):
-        from magma_gb300.batched import PRECISIONS
+        from magma_gb300.batched import PRECISIONS, SOLVERS
         b, n, r = self.batch, self.n, self.nrhs
-        rc = c["lib"].magma_dxgesv_batched_work(
-            PRECISIONS[self.precision], n, r, vp(c["dSs"][i]), n, vp(c["dipiv"]), vp(c["dB"]), n,
-            vp(c["dX"]), n, vp(c["info"]), vp(c["iter"]), self.itermax, self.tol, 1,
-            vp(c["work"]), C.byref(c["lwork"]), b, c["q"].handle)
+        rc = c["lib"].magma_dxgesv_gmres_batched_work(
+            PRECISIONS[self.precision], SOLVERS[self.solver], n, r, vp(c["dSs"][i]), n,
+            vp(c["dipiv"]), vp(c["dB"]), n, vp(c["dX"]), n, vp(c["info"]), vp(c["iter"]),
+            self.itermax, self.tol, 1, vp(c["work"]), C.byref(c["lwork"]), b, c["q"].handle)
         if rc != 0:
-            raise RuntimeError(f"magma_dxgesv_batched_work({self.precision}) returned {rc}")
+            raise RuntimeError(f"magma_dxgesv_gmres_batched_work({self.precision}, {self.solver}) "
+                               f"returned {rc}")
 
     dominant_class = "ir_residual"
     dominant = "mlu::ir_residual_kernel<4> (FP64 residual R = B - A X)"
@@ -1240,6 +1247,8 @@ def main():
                     help="run warm-up and timed launches only (for ncu), print nothing")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "bf16"],
                     help="dsgesv512: factorisation precision of the refinement")
+    ap.add_argument("--solver", default="ir", choices=["ir", "gmres"],
+                    help="dsgesv512: refinement solver (gmres: Magma_REFINE_IRGMSTRS)")
     ap.add_argument("--batch", type=int, default=None,
                     help="with --profile: run the workload on its first BATCH matrices "
                          "(a small case for full ncu captures)")
@@ -1249,6 +1258,11 @@ def main():
         if args.workload != "dsgesv512":
             ap.error("--precision applies to the dsgesv512 workload")
         wl.precision = args.precision
+    if args.solver != "ir":
+        if args.workload != "dsgesv512":
+            ap.error("--solver applies to the dsgesv512 workload")
+        wl.solver = args.solver
+        wl.itermax = 10     # the reference's outer limit for Magma_REFINE_IRGMSTRS at n = 512
     if args.batch is not None:
         if not args.profile:
             ap.error("--batch is only for --profile runs")

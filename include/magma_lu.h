@@ -445,6 +445,39 @@ magma_int_t magma_dxgesv_batched_work(magma_int_t precision, magma_int_t n, magm
                                       void *work, size_t *lwork,
                                       magma_int_t batchCount, magma_queue_t queue);
 
+/* Batched form of magma_dxgesv_gmres_gpu (src/dxgesv_gmres_gpu.cpp:160-170,
+ * declared in include/magma_htc.h) for the two refinement solvers that use a
+ * low-precision LU: solver_type 920 (Magma_REFINE_IRSTRS, include/
+ * magma_types.h:873) is magma_dxgesv_batched_work; 922 (Magma_REFINE_IRGMSTRS)
+ * solves each refinement iteration's correction equation A d = r with GMRES
+ * right-preconditioned by the factors (at most min(n, 50) inner iterations,
+ * stop at a 1e-4 relative reduction, as the reference's inner FGMRES) instead
+ * of one solve.  The residual, update and stopping rule stay in FP64 (as
+ * magma_dxgesv_batched_work); the inner GMRES runs in FP32 on an FP32 copy of
+ * A.  diter_array reports, for a converged matrix, the total of its inner
+ * iteration counts (the largest over its right-hand sides in each refinement
+ * iteration), as the reference's iter for these solvers; the other codes are
+ * those of magma_dxgesv_batched_work, itermax bounding the refinement
+ * iterations (the reference uses max(10, min(n, 500) / 50) for this solver).
+ * Unlike the reference, a refinement step after which the residual 2-norm of
+ * some right-hand side has not at least halved ends that matrix's refinement
+ * (iter -itermax-1, then the FP64 re-solve when fallback is set).  922 takes
+ * nrhs <= 8 and uniform sizes.  Other arguments,
+ * workspace query and errors as magma_dxgesv_batched_work, shifted by two;
+ * -1 precision, -2 solver_type, -4 nrhs above 8 for 922. */
+#define Magma_REFINE_IRSTRS 920
+#define Magma_REFINE_IRGMSTRS 922
+magma_int_t magma_dxgesv_gmres_batched_work(magma_int_t precision, magma_int_t solver_type,
+                                            magma_int_t n, magma_int_t nrhs,
+                                            double **dA_array, magma_int_t ldda,
+                                            magma_int_t **dipiv_array,
+                                            double **dB_array, magma_int_t lddb,
+                                            double **dX_array, magma_int_t lddx,
+                                            magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                            magma_int_t itermax, double tol, magma_int_t fallback,
+                                            void *work, size_t *lwork,
+                                            magma_int_t batchCount, magma_queue_t queue);
+
 /* No counterpart in the reference: the batched refinement of
  * magma_dxgesv_batched_work for a variable-size batch.  n[k], nrhs[k], ldda[k],
  * lddb[k] and lddx[k] are device arrays; max_n and max_nrhs (<= 16) are their

@@ -171,13 +171,16 @@ def dsgesv_batched(S: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = No
                    itermax: int = 30, tol: float = 0.0, fallback: bool = True,
                    ipiv: torch.Tensor | None = None, info: torch.Tensor | None = None,
                    iters: torch.Tensor | None = None, work: torch.Tensor | None = None,
-                   queue: Queue | None = None, precision: str = "fp32"):
+                   queue: Queue | None = None, precision: str = "fp32", solver: str = "ir"):
     """Batched FP32-factor / FP64-refinement solve (magma_dsgesv_batched_work).
 
     S and B are FP64 column-major storage and are left unchanged unless a
     matrix falls back to FP64 (then S holds its FP64 LU).  Returns
     (X, ipiv, info, iters).  `work` may be a preallocated uint8 CUDA tensor of
-    at least dsgesv_workspace_bytes() bytes."""
+    at least dsgesv_workspace_bytes() bytes.  solver "gmres" solves each
+    correction with GMRES preconditioned by the factors
+    (magma_dxgesv_gmres_batched_work, Magma_REFINE_IRGMSTRS); iters then
+    counts inner iterations."""
     _check_storage(S, "S")
     _check_storage(B, "B")
     if S.dtype != torch.float64 or B.dtype != torch.float64:
@@ -192,25 +195,31 @@ def dsgesv_batched(S: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = No
     q = queue or Queue.current(S.device)
     lib = _L.load()
     prec = PRECISIONS[precision]
-    need = dsgesv_workspace_bytes(n, nrhs, b, precision)
+    need = dsgesv_workspace_bytes(n, nrhs, b, precision, solver)
     if work is None or work.numel() < need:
         work = torch.empty((max(need, 1),), dtype=torch.uint8, device=S.device)
     lw = C.c_size_t(work.numel())
     dA, dP, dB, dX = ptr_array(S), ptr_array(ipiv), ptr_array(B), ptr_array(X)
-    rc = lib.magma_dxgesv_batched_work(prec, n, nrhs, _vp(dA), ld, _vp(dP), _vp(dB), ldb, _vp(dX),
-                                       X.shape[2], _vp(info), _vp(iters), itermax, float(tol),
-                                       1 if fallback else 0, _vp(work), C.byref(lw), b, q.handle)
-    _check(rc, "magma_dxgesv_batched_work")
+    rc = lib.magma_dxgesv_gmres_batched_work(prec, SOLVERS[solver], n, nrhs, _vp(dA), ld, _vp(dP),
+                                             _vp(dB), ldb, _vp(dX), X.shape[2], _vp(info),
+                                             _vp(iters), itermax, float(tol), 1 if fallback else 0,
+                                             _vp(work), C.byref(lw), b, q.handle)
+    _check(rc, "magma_dxgesv_gmres_batched_work")
     return X, ipiv, info, iters
 
 
-def dsgesv_workspace_bytes(n: int, nrhs: int, batch: int, precision: str = "fp32") -> int:
+SOLVERS = {"ir": 920, "gmres": 922}
+
+
+def dsgesv_workspace_bytes(n: int, nrhs: int, batch: int, precision: str = "fp32",
+                           solver: str = "ir") -> int:
     lib = _L.load()
     lw = C.c_size_t(0)
-    rc = lib.magma_dxgesv_batched_work(PRECISIONS[precision], n, nrhs, None, max(n, 1), None,
-                                       None, max(n, 1), None, max(n, 1), None, None, 30, 0.0, 0,
-                                       None, C.byref(lw), batch, None)
-    _check(rc, "magma_dsgesv_batched_work(query)")
+    rc = lib.magma_dxgesv_gmres_batched_work(PRECISIONS[precision], SOLVERS[solver], n, nrhs, None,
+                                             max(n, 1), None, None, max(n, 1), None, max(n, 1),
+                                             None, None, 30, 0.0, 0, None, C.byref(lw), batch,
+                                             None)
+    _check(rc, "magma_dxgesv_gmres_batched_work(query)")
     return int(lw.value)
 
 

@@ -491,8 +491,310 @@ ir_residual_kernel(IrShape sh, double **dA_array, double **dB_array, double **dX
     atomic_max_nonneg(&nm[2 * IR_NRHS_MAX + 1], xrow);
 }
 
+// ---------------------------------------------------------------------------
+// GMRES-based refinement (Magma_REFINE_IRGMSTRS of magma_dxgesv_gmres_gpu,
+// src/dxgesv_gmres_gpu.cpp:604-780): each refinement iteration solves the
+// correction equation A d = r with GMRES right-preconditioned by the
+// low-precision LU factors (the reference: FGMRES, src/dgmres_plu_gpu.cpp,
+// restart = inner_itermax = 50, relative tolerance innertol = 1e-4, x0 = 0,
+// modified Gram-Schmidt, Givens rotations) instead of one solve with them.
+// The residual, the update and the stopping rule stay in FP64; the inner
+// GMRES runs in FP32 (an FP32 copy of A, FP32 Krylov vectors): FP64 runs at
+// 1/64 of the FP32 rate here, and an FP32 inner solver still refines to FP64
+// accuracy for condition numbers up to about 1/u_single.  One CTA per matrix
+// runs a whole inner solve (at most 8 right-hand sides, one Krylov process
+// each), so a refinement iteration is one launch.
+constexpr int GM_INNER_MAX = 50;
+constexpr float GM_INNER_TOL = 1e-4f;
+constexpr int GM_THREADS = 256;
+constexpr int GM_WARPS = GM_THREADS / 32;
+constexpr int GM_NRHS_MAX = 8;
+// A refinement step whose residual 2-norm did not at least halve (any
+// right-hand side) ends the refinement of that matrix: it is marked as not
+// converged and goes to the FP64 re-solve (the reference instead runs all its
+// outer iterations; with FP16/BF16 factors at kappa ~1e6 the GMRES correction
+// stalls and every further iteration is wasted).
+constexpr double GM_STALL = 0.5;
+
+// A32 = float(A) (uniform batch, rows coalesced)
+__global__ void __launch_bounds__(IR_ROWS)
+gm_a32_kernel(IrShape sh, double **dA_array, float *A32, int ldas)
+{
+    const int mat = blockIdx.y;
+    const int i = blockIdx.x * IR_ROWS + threadIdx.x;
+    if (i >= sh.n) return;
+    const double *A = dA_array[mat];
+    float *D = A32 + (size_t)mat * sh.n * ldas;
+    for (int j = 0; j < sh.n; j++) D[i + (size_t)j * ldas] = __double2float_rn(A[i + (size_t)j * sh.lda]);
+}
+
+// Block sums of NR per-thread partials, lane order then warp order (the same
+// order on every call); the sums land in out[] for every thread.
+template <typename F, int NR>
+__device__ __forceinline__ void gm_block_sum(F (&v)[NR], F (*red)[NR], F *out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NR; c++) {
+        F x = v[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+        v[c] = x;
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < NR; c++) red[warp][c] = v[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < NR) {
+        F t = F(0);
+        for (int w = 0; w < GM_WARPS; w++) t += red[w][threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
+template <int NR>
+__host__ __device__ inline size_t gm_smem_bytes(int n)
+{
+    const int m = n < GM_INNER_MAX ? n : GM_INNER_MAX;
+    return sizeof(float) * ((size_t)2 * NR * n + (size_t)NR * (m + 1) * m + (size_t)NR * (3 * m + 1));
+}
+
+// check (as ir_solve_kernel) + GMRES correction X += d for the nrhs <= NR
+// right-hand sides of one matrix.  V: per right-hand side GM_INNER_MAX+1 FP32
+// vectors of n.
+template <int NR>
+__global__ void __launch_bounds__(GM_THREADS)
+gm_correction_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, const float *A32,
+                     double **dX_array, const double *R, unsigned long long *stats, int *iter,
+                     int *inner_total, int it, double tol, const double *rowscale,
+                     const double *colscale, float *Vbase, double *beta_prev, int itermax)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float s_red[GM_WARPS][NR], s_sum[NR];
+    __shared__ double s_red64[GM_WARPS][NR], s_sum64[NR];
+    __shared__ int s_go, s_act[NR], s_k[NR], s_any;
+    const int mat = blockIdx.y, tid = threadIdx.x;
+    const int n = sh.N(mat), nrhs = sh.NR(mat), lddx = sh.LDX(mat);
+    if (n == 0 || nrhs == 0) return;
+    const int m = min(GM_INNER_MAX, n);
+    float *sB = reinterpret_cast<float *>(smem_raw);   // [NR][n]: preconditioner input / output
+    float *sW = sB + NR * n;                           // [NR][n]: Arnoldi vector
+    float *sH = sW + NR * n;                           // [NR][m+1][m]: Hessenberg matrices
+    float *sCs = sH + NR * (m + 1) * m;                // [NR][m]
+    float *sSn = sCs + NR * m;                         // [NR][m]
+    float *sRs = sSn + NR * m;                         // [NR][m+1]: rotated right-hand side, then y
+    unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
+    if (tid == 0) {
+        int go = st[1] == IR_ACTIVE;
+        if (go && ir_converged(st, it & 1, n, nrhs, tol)) {
+            go = 0;
+            st[1] = IR_CONVERGED;
+            iter[mat] = inner_total[mat];
+        }
+        s_go = go;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    {
+        unsigned long long *nx = norms_of(st, (it + 1) & 1);
+        for (int e = tid; e < 2 * IR_NRHS_MAX + 2; e += GM_THREADS) nx[e] = 0ull;
+    }
+    const int nr = min(NR, nrhs);
+    const double *Rm = R + (size_t)mat * sh.nrhs * sh.n;
+    float *Vm = Vbase + (size_t)mat * sh.nrhs * (GM_INNER_MAX + 1) * sh.n;
+    const int *pm = perm + (size_t)mat * sh.n;
+    const float *Am = A32 + (size_t)mat * sh.n * ldas;
+    const float *LU = dAs_array[mat];
+    const double *rsc = rowscale ? rowscale + (size_t)mat * sh.n : nullptr;
+    const double *csc = colscale ? colscale + (size_t)mat * sh.n : nullptr;
+    auto V = [&](int c, int j) { return Vm + ((size_t)c * (GM_INNER_MAX + 1) + j) * sh.n; };
+
+    // beta_c = ||r_c||_2 in FP64; v_0 = r_c / beta_c; the inner system is
+    // A z = v_0 with ||v_0|| = 1 (rs_0 = 1), and d = beta_c z
+    {
+        double part[NR];
+#pragma unroll
+        for (int c = 0; c < NR; c++) part[c] = 0.0;
+        for (int r = tid; r < n; r += GM_THREADS)
+#pragma unroll
+            for (int c = 0; c < NR; c++)
+                if (c < nr) { const double x = Rm[r + (size_t)c * sh.n]; part[c] = fma(x, x, part[c]); }
+        gm_block_sum<double, NR>(part, s_red64, s_sum64);
+    }
+    double beta[NR];
+#pragma unroll
+    for (int c = 0; c < NR; c++) beta[c] = sqrt(s_sum64[c]);
+    if (tid == 0) {
+        double *bp = beta_prev + (size_t)mat * NR;
+        int stall = 0;
+        for (int c = 0; c < nr; c++) {
+            if (it > 0 && !(beta[c] <= GM_STALL * bp[c])) stall = 1;
+            bp[c] = beta[c];
+        }
+        if (stall) {
+            st[1] = IR_FAILED;
+            iter[mat] = -itermax - 1;
+        }
+        s_go = !stall;
+    }
+    __syncthreads();
+    if (!s_go) return;
+    for (int r = tid; r < n; r += GM_THREADS)
+#pragma unroll
+        for (int c = 0; c < NR; c++)
+            if (c < nr) V(c, 0)[r] = beta[c] > 0.0 ? __double2float_rn(Rm[r + (size_t)c * sh.n] / beta[c]) : 0.f;
+    if (tid < NR) {
+        s_act[tid] = tid < nr && beta[tid] > 0.0 && isfinite(beta[tid]);
+        s_k[tid] = 0;
+        sRs[tid * (m + 1)] = 1.f;
+    }
+    __syncthreads();
+    for (int i = 0; i < m; i++) {
+        if (tid == 0) {
+            int a = 0;
+#pragma unroll
+            for (int c = 0; c < NR; c++) a |= s_act[c];
+            s_any = a;
+        }
+        __syncthreads();
+        if (!s_any) break;
+        // z = M^{-1} v_i: row interchanges (and the FP16 form's row scale) on
+        // the way in, the column scale on the way out
+        for (int e = tid; e < NR * n; e += GM_THREADS) {
+            const int c = e / n, q = e % n, p = pm[q];
+            float x = 0.f;
+            if (c < nr) {
+                x = V(c, i)[p];
+                if (rsc) x *= (float)rsc[p];
+            }
+            sB[c * n + q] = x;
+        }
+        __syncthreads();
+        solve_smem<float, false, NR>(n, LU, ldas, nullptr, sB, nr);
+        __syncthreads();
+        if (csc) {
+            for (int e = tid; e < NR * n; e += GM_THREADS) sB[e] *= (float)csc[e % n];
+            __syncthreads();
+        }
+        // w = A z
+        for (int r = tid; r < n; r += GM_THREADS) {
+            float acc[NR];
+#pragma unroll
+            for (int c = 0; c < NR; c++) acc[c] = 0.f;
+            const float *Ar = Am + r;
+#pragma unroll 8
+            for (int j = 0; j < n; j++) {
+                const float a = Ar[(size_t)j * ldas];
+#pragma unroll
+                for (int c = 0; c < NR; c++) acc[c] = fmaf(a, sB[c * n + j], acc[c]);
+            }
+#pragma unroll
+            for (int c = 0; c < NR; c++) sW[c * n + r] = acc[c];
+        }
+        // modified Gram-Schmidt against v_0..v_i
+        for (int j = 0; j <= i; j++) {
+            float part[NR];
+#pragma unroll
+            for (int c = 0; c < NR; c++) part[c] = 0.f;
+            for (int r = tid; r < n; r += GM_THREADS)
+#pragma unroll
+                for (int c = 0; c < NR; c++)
+                    if (c < nr) part[c] = fmaf(sW[c * n + r], V(c, j)[r], part[c]);
+            gm_block_sum<float, NR>(part, s_red, s_sum);
+            for (int r = tid; r < n; r += GM_THREADS)
+#pragma unroll
+                for (int c = 0; c < NR; c++)
+                    if (c < nr) sW[c * n + r] = fmaf(-s_sum[c], V(c, j)[r], sW[c * n + r]);
+            if (tid < NR) sH[((size_t)tid * (m + 1) + j) * m + i] = s_sum[tid];
+        }
+        {
+            float part[NR];
+#pragma unroll
+            for (int c = 0; c < NR; c++) part[c] = 0.f;
+            for (int r = tid; r < n; r += GM_THREADS)
+#pragma unroll
+                for (int c = 0; c < NR; c++)
+                    if (c < nr) part[c] = fmaf(sW[c * n + r], sW[c * n + r], part[c]);
+            gm_block_sum<float, NR>(part, s_red, s_sum);
+        }
+        float hn[NR];
+#pragma unroll
+        for (int c = 0; c < NR; c++) hn[c] = sqrtf(s_sum[c]);
+        if (i + 1 <= m)
+            for (int r = tid; r < n; r += GM_THREADS)
+#pragma unroll
+                for (int c = 0; c < NR; c++)
+                    if (c < nr) V(c, i + 1)[r] = hn[c] > 0.f ? sW[c * n + r] / hn[c] : 0.f;
+        if (tid < NR) sH[((size_t)tid * (m + 1) + i + 1) * m + i] = hn[tid];
+        __syncthreads();
+        // Givens rotations, one thread per right-hand side
+        if (tid < nr && s_act[tid]) {
+            const int c = tid;
+            float *H = sH + (size_t)c * (m + 1) * m;
+            float *cs = sCs + c * m, *sn = sSn + c * m, *rs = sRs + c * (m + 1);
+            for (int j = 0; j < i; j++) {
+                const float t = H[j * m + i], u = H[(j + 1) * m + i];
+                H[j * m + i] = cs[j] * t + sn[j] * u;
+                H[(j + 1) * m + i] = -sn[j] * t + cs[j] * u;
+            }
+            const float a = H[i * m + i], b = H[(i + 1) * m + i];
+            float gam = hypotf(a, b);
+            if (gam == 0.f) gam = 1e-30f;
+            cs[i] = a / gam;
+            sn[i] = b / gam;
+            rs[i + 1] = -sn[i] * rs[i];
+            rs[i] = cs[i] * rs[i];
+            H[i * m + i] = cs[i] * a + sn[i] * b;
+            s_k[c] = i + 1;
+            if (!(fabsf(rs[i + 1]) > GM_INNER_TOL) || b == 0.f) s_act[c] = 0;
+        }
+        __syncthreads();
+    }
+    // y = H^{-1} rs (upper triangular, k x k)
+    if (tid < nr && s_k[tid] > 0) {
+        const int c = tid, k = s_k[c];
+        const float *H = sH + (size_t)c * (m + 1) * m;
+        float *rs = sRs + c * (m + 1);
+        for (int kk = k - 1; kk >= 0; kk--) {
+            float t = rs[kk];
+            for (int j = kk + 1; j < k; j++) t = fmaf(-H[kk * m + j], rs[j], t);
+            rs[kk] = t / H[kk * m + kk];
+        }
+    }
+    __syncthreads();
+    // d = beta M^{-1} (V y)
+    for (int e = tid; e < NR * n; e += GM_THREADS) {
+        const int c = e / n, q = e % n, p = pm[q];
+        float t = 0.f;
+        if (c < nr) {
+            for (int j = 0; j < s_k[c]; j++) t = fmaf(sRs[c * (m + 1) + j], V(c, j)[p], t);
+            if (rsc) t *= (float)rsc[p];
+        }
+        sB[c * n + q] = t;
+    }
+    __syncthreads();
+    solve_smem<float, false, NR>(n, LU, ldas, nullptr, sB, nr);
+    __syncthreads();
+    double *X = dX_array[mat];
+    for (int e = tid; e < nr * n; e += GM_THREADS) {
+        const int c = e / n, q = e % n;
+        if (s_k[c] == 0) continue;
+        const double d = (double)sB[c * n + q];
+        X[q + (size_t)c * lddx] += beta[c] * (csc ? d * csc[q] : d);
+    }
+    if (tid == 0) {
+        int kmax = 0;
+#pragma unroll
+        for (int c = 0; c < NR; c++) kmax = max(kmax, s_k[c]);
+        inner_total[mat] += kmax;
+    }
+}
+
 __global__ void ir_final_kernel(IrShape sh, unsigned long long *stats, int *iter, int itermax,
-                                double tol, int batch, int *failed_count)
+                                double tol, int batch, int *failed_count,
+                                const int *inner_total = nullptr)
 {
     const int mat = blockIdx.x * blockDim.x + threadIdx.x;
     if (mat >= batch) return;
@@ -500,7 +802,7 @@ __global__ void ir_final_kernel(IrShape sh, unsigned long long *stats, int *iter
     if (st[1] == IR_ACTIVE) {
         if (ir_converged(st, itermax & 1, sh.N(mat), sh.NR(mat), tol)) {
             st[1] = IR_CONVERGED;
-            iter[mat] = itermax;
+            iter[mat] = inner_total ? inner_total[mat] : itermax;
         } else {
             st[1] = IR_FAILED;
             iter[mat] = -itermax - 1;
@@ -562,13 +864,14 @@ static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct IrLayout {
     size_t stats, count, asp, as, r, perm, ca, cp, cx, cidx, cinfo, rsc, csc, tc, tc_bytes;
-    size_t ldas_arr, csize, vbw, ca2, cp2, csize2, total;
+    size_t ldas_arr, csize, vbw, ca2, cp2, csize2, gm_a32, gm_v, gm_inner, gm_beta, total;
     int ldas;
 };
 
 // Workspace of a refinement over `batch` matrices of order <= n with <= nrhs
 // right-hand sides; `vb` adds the arrays of a variable-size batch.
-static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900, bool vb = false)
+static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900, bool vb = false,
+                          int solver = 920)
 {
     IrLayout L;
     L.ldas = (n + 31) & ~31;
@@ -607,6 +910,13 @@ static IrLayout ir_layout(int n, int nrhs, int batch, int prec = 900, bool vb = 
         L.tc = o;
         L.tc_bytes = tcb;
         o = align256(o + tcb);
+    }
+    L.gm_a32 = L.gm_v = L.gm_inner = L.gm_beta = o;
+    if (solver == 922) {   // GMRES refinement: FP32 copy of A, Krylov vectors, inner counts
+        L.gm_a32 = o;   o = align256(o + (size_t)batch * n * L.ldas * sizeof(float));
+        L.gm_v = o;     o = align256(o + (size_t)batch * nrhs * (GM_INNER_MAX + 1) * n * sizeof(float));
+        L.gm_inner = o; o = align256(o + (size_t)batch * sizeof(int));
+        L.gm_beta = o;  o = align256(o + (size_t)batch * GM_NRHS_MAX * sizeof(double));
     }
     L.total = o;
     return L;
@@ -653,6 +963,15 @@ static void correction_solve(const IrShape &sh, float **As_array, int ldas, cons
             sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, rsc, csc));
 }
 
+static size_t gm_dyn_max()
+{
+    static size_t v = 0;
+    if (!v)
+        v = min(mlu_allow_dynamic_smem(gm_correction_kernel<4>),
+                mlu_allow_dynamic_smem(gm_correction_kernel<8>));
+    return v;
+}
+
 static size_t solve_dyn_max()
 {
     static size_t v = 0;
@@ -678,11 +997,12 @@ static magma_int_t
 ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array,
        double **dB_array, double **dX_array, magma_int_t *dinfo_array, magma_int_t *diter_array,
        magma_int_t itermax, double tol, magma_int_t fallback, void *work, size_t *lwork,
-       magma_int_t batchCount, magma_queue_t queue)
+       magma_int_t batchCount, magma_queue_t queue, int solver = 920)
 {
     const bool vb = sh.n_arr != nullptr;
     const int n = sh.n, nrhs = sh.nrhs;
-    const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0), prec, vb);
+    const bool gm = solver == 922;
+    const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0), prec, vb, solver);
     if (work == nullptr) {          // workspace query
         *lwork = L.total;
         return 0;
@@ -692,6 +1012,8 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
     // shared-memory limits of the correction solve and the residual kernels
     if ((size_t)IR_SOLVE_NR * n * sizeof(float) > solve_dyn_max() ||
         (size_t)n * IR_NRHS_MAX * sizeof(double) > 200 * 1024)
+        return MAGMA_ERR_NOT_SUPPORTED;
+    if (gm && (vb || nrhs > GM_NRHS_MAX || gm_smem_bytes<GM_NRHS_MAX>(n) > gm_dyn_max()))
         return MAGMA_ERR_NOT_SUPPORTED;
 
     cudaStream_t s = queue->stream;
@@ -734,14 +1056,36 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
         correction_solve<false>(sh, As_array, L.ldas, perm, dX_array, R, stats, diter_array,
                                 dinfo_array, it, tol, rsc, csc, batchCount, s);
     };
+    float *A32 = gm ? (float *)(w + L.gm_a32) : nullptr;
+    float *Vk = gm ? (float *)(w + L.gm_v) : nullptr;
+    int *inner = gm ? (int *)(w + L.gm_inner) : nullptr;
+    double *beta_prev = gm ? (double *)(w + L.gm_beta) : nullptr;
+    if (gm) {
+        cudaMemsetAsync(inner, 0, (size_t)batchCount * sizeof(int), s);
+        MLU_LAUNCH(mlu::KC_IR_INIT, s, gm_a32_kernel<<<rows_grid, IR_ROWS, 0, s>>>(
+            sh, dA_array, A32, L.ldas));
+    }
+    auto gmres = [&](int it) {
+        if (nrhs <= 4)
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, gm_correction_kernel<4><<<dim3(1, batchCount), GM_THREADS,
+                                                                      gm_smem_bytes<4>(n), s>>>(
+                sh, As_array, L.ldas, perm, A32, dX_array, R, stats, diter_array, inner, it, tol,
+                rsc, csc, Vk, beta_prev, itermax));
+        else
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, gm_correction_kernel<8><<<dim3(1, batchCount), GM_THREADS,
+                                                                      gm_smem_bytes<8>(n), s>>>(
+                sh, As_array, L.ldas, perm, A32, dX_array, R, stats, diter_array, inner, it, tol,
+                rsc, csc, Vk, beta_prev, itermax));
+    };
     solve(-1);
     residual<false>(sh, dA_array, dB_array, dX_array, R, stats, 0, batchCount, s);
     for (int it = 0; it < itermax; it++) {
-        solve(it);
+        if (gm) gmres(it);
+        else solve(it);
         residual<false>(sh, dA_array, dB_array, dX_array, R, stats, (it + 1) & 1, batchCount, s);
     }
     MLU_LAUNCH(mlu::KC_OTHER, s, ir_final_kernel<<<mlu_ceildiv(batchCount, 256), 256, 0, s>>>(
-        sh, stats, diter_array, itermax, tol, batchCount, count));
+        sh, stats, diter_array, itermax, tol, batchCount, count, inner));
     MLU_CHECK_LAUNCH();
     if (!fallback) return 0;
 
@@ -904,7 +1248,7 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
           magma_int_t ldda, magma_int_t **dipiv_array, double **dB_array, magma_int_t lddb,
           double **dX_array, magma_int_t lddx, magma_int_t *dinfo_array, magma_int_t *diter_array,
           magma_int_t itermax, double tol, magma_int_t fallback, void *work, size_t *lwork,
-          magma_int_t batchCount, magma_queue_t queue)
+          magma_int_t batchCount, magma_queue_t queue, int solver = 920)
 {
     magma_int_t info = 0;
     if (n < 0) info = -1;
@@ -919,7 +1263,7 @@ ir_driver(const char *name, int argoff, int prec, magma_int_t n, magma_int_t nrh
     }
     const IrShape sh = {n, nrhs, ldda, lddb, lddx, nullptr, nullptr, nullptr, nullptr, nullptr};
     return ir_run(prec, sh, dA_array, dipiv_array, dB_array, dX_array, dinfo_array, diter_array,
-                  itermax, tol, fallback, work, lwork, batchCount, queue);
+                  itermax, tol, fallback, work, lwork, batchCount, queue, solver);
 }
 
 extern "C" magma_int_t
@@ -951,6 +1295,29 @@ magma_dxgesv_batched_work(magma_int_t precision, magma_int_t n, magma_int_t nrhs
     return ir_driver(__func__, 1, precision, n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb,
                      dX_array, lddx, dinfo_array, diter_array, itermax, tol, fallback, work, lwork,
                      batchCount, queue);
+}
+
+extern "C" magma_int_t
+magma_dxgesv_gmres_batched_work(magma_int_t precision, magma_int_t solver_type, magma_int_t n,
+                                magma_int_t nrhs, double **dA_array, magma_int_t ldda,
+                                magma_int_t **dipiv_array, double **dB_array, magma_int_t lddb,
+                                double **dX_array, magma_int_t lddx, magma_int_t *dinfo_array,
+                                magma_int_t *diter_array, magma_int_t itermax, double tol,
+                                magma_int_t fallback, void *work, size_t *lwork,
+                                magma_int_t batchCount, magma_queue_t queue)
+{
+    magma_int_t info = 0;
+    if (precision != 900 && precision != 905 && precision != 930) info = -1;
+    else if (solver_type != 920 && solver_type != 922) info = -2;
+    else if (solver_type == 922 && (nrhs < 0 || nrhs > GM_NRHS_MAX)) info = -4;
+    if (info != 0) {
+        magma_xerbla(__func__, -info);
+        return info;
+    }
+    // argument i of magma_dsgesv_batched_work is argument i+2 here
+    return ir_driver(__func__, 2, precision, n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb,
+                     dX_array, lddx, dinfo_array, diter_array, itermax, tol, fallback, work, lwork,
+                     batchCount, queue, (int)solver_type);
 }
 
 extern "C" magma_int_t

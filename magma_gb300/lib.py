@@ -128,6 +128,9 @@ for _p in "ds":
                                             c_ptr], c_int)
     _PROTOS[f"magma_{_p}posv_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr,
                                            c_int, c_ptr], c_int)
+_PROTOS["magma_dxgesv_gmres_batched_work"] = ([c_int, c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_ptr,
+                                               c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, C.c_double,
+                                               c_int, c_ptr, c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
 _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],

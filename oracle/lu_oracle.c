@@ -225,8 +225,127 @@ int oracle_max_threads(void)
  *   refinements; not converged: iter = -itermax-1.  When iter < 0 and
  *   fallback is set, A is overwritten by its FP64 LU and X solved in FP64.
  * Returns info. */
+/* GMRES correction of the GMRES-based refinement (the GPU's
+ * gm_correction_kernel; the reference's Magma_REFINE_IRGMSTRS,
+ * src/dxgesv_gmres_gpu.cpp:604-780 with src/dgmres_plu_gpu.cpp): for each
+ * column r of R, beta = ||r||_2 (FP64), then GMRES in FP32 on A z = r/beta,
+ * right-preconditioned by the FP32 factors (sgetrs), x0 = 0, at most
+ * min(n, 50) iterations, modified Gram-Schmidt, Givens rotations, stop when
+ * the rotated residual |rs| <= 1e-4 (relative, rs_0 = 1) or on breakdown;
+ * y from the triangular system, X += beta * sgetrs(V y).  A32 = (float)A.
+ * Dot products are summed in index order (the GPU sums per thread, then
+ * across threads), so the two agree to FP32 rounding, not bit for bit.
+ * Returns the largest inner iteration count over the columns. */
+static int gmres_correction(int n, int nrhs, const float *A32, const float *As, const int *ipiv,
+                            const double *R, double *X, int ldx, double *beta_prev, int first,
+                            int *stalled)
+{
+    const int m = n < 50 ? n : 50;
+    float *V = (float *)malloc(sizeof(float) * (size_t)(m + 1) * n + 4);
+    float *H = (float *)malloc(sizeof(float) * (size_t)(m + 1) * m + 4);
+    float *cs = (float *)malloc(sizeof(float) * (m + 1)), *sn = (float *)malloc(sizeof(float) * (m + 1));
+    float *rs = (float *)malloc(sizeof(float) * (m + 2));
+    float *w = (float *)malloc(sizeof(float) * (size_t)n + 4), *z = (float *)malloc(sizeof(float) * (size_t)n + 4);
+    int kmax = 0;
+    /* a right-hand side whose residual 2-norm did not at least halve since the
+     * previous correction ends the refinement (the GPU's GM_STALL rule) */
+    *stalled = 0;
+    for (int c = 0; c < nrhs; c++) {
+        const double *r = R + (size_t)c * n;
+        double b2 = 0.0;
+        for (int i = 0; i < n; i++) b2 = fma(r[i], r[i], b2);
+        const double beta = sqrt(b2);
+        if (!first && !(beta <= 0.5 * beta_prev[c])) *stalled = 1;
+        beta_prev[c] = beta;
+    }
+    if (*stalled) goto done;
+    for (int c = 0; c < nrhs; c++) {
+        const double *r = R + (size_t)c * n;
+        const double beta = beta_prev[c];
+        if (!(beta > 0.0) || isinf(beta)) continue;
+        for (int i = 0; i < n; i++) V[i] = (float)(r[i] / beta);
+        rs[0] = 1.0f;
+        int k = 0;
+        for (int it = 0; it < m; it++) {
+            float *vi = V + (size_t)it * n;
+            for (int i = 0; i < n; i++) z[i] = vi[i];
+            oracle_sgetrs(0, n, 1, As, n, ipiv, z, n);
+            for (int i = 0; i < n; i++) {
+                float acc = 0.0f;
+                for (int j = 0; j < n; j++) acc = fmaf(A32[i + (size_t)j * n], z[j], acc);
+                w[i] = acc;
+            }
+            for (int j = 0; j <= it; j++) {
+                const float *vj = V + (size_t)j * n;
+                float h = 0.0f;
+                for (int i = 0; i < n; i++) h = fmaf(w[i], vj[i], h);
+                for (int i = 0; i < n; i++) w[i] = fmaf(-h, vj[i], w[i]);
+                H[j * m + it] = h;
+            }
+            float hn2 = 0.0f;
+            for (int i = 0; i < n; i++) hn2 = fmaf(w[i], w[i], hn2);
+            const float hn = sqrtf(hn2);
+            float *vn = V + (size_t)(it + 1) * n;
+            for (int i = 0; i < n; i++) vn[i] = hn > 0.0f ? w[i] / hn : 0.0f;
+            H[(it + 1) * m + it] = hn;
+            for (int j = 0; j < it; j++) {
+                const float t = H[j * m + it], u = H[(j + 1) * m + it];
+                H[j * m + it] = cs[j] * t + sn[j] * u;
+                H[(j + 1) * m + it] = -sn[j] * t + cs[j] * u;
+            }
+            const float a = H[it * m + it], bb = H[(it + 1) * m + it];
+            float gam = hypotf(a, bb);
+            if (gam == 0.0f) gam = 1e-30f;
+            cs[it] = a / gam;
+            sn[it] = bb / gam;
+            rs[it + 1] = -sn[it] * rs[it];
+            rs[it] = cs[it] * rs[it];
+            H[it * m + it] = cs[it] * a + sn[it] * bb;
+            k = it + 1;
+            if (!(fabsf(rs[it + 1]) > 1e-4f) || bb == 0.0f) break;
+        }
+        for (int kk = k - 1; kk >= 0; kk--) {
+            float t = rs[kk];
+            for (int j = kk + 1; j < k; j++) t = fmaf(-H[kk * m + j], rs[j], t);
+            rs[kk] = t / H[kk * m + kk];
+        }
+        for (int i = 0; i < n; i++) {
+            float t = 0.0f;
+            for (int j = 0; j < k; j++) t = fmaf(rs[j], V[(size_t)j * n + i], t);
+            z[i] = t;
+        }
+        oracle_sgetrs(0, n, 1, As, n, ipiv, z, n);
+        for (int i = 0; i < n; i++) X[i + (size_t)c * ldx] += beta * (double)z[i];
+        if (k > kmax) kmax = k;
+    }
+done:
+    free(V); free(H); free(cs); free(sn); free(rs); free(w); free(z);
+    return kmax;
+}
+
+static int dsgesv_impl(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
+                       int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out,
+                       int gmres);
+
 int oracle_dsgesv(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
                   int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out)
+{
+    return dsgesv_impl(n, nrhs, A, lda, B, ldb, X, ldx, ipiv, itermax, tol, fallback, iter_out, 0);
+}
+
+/* The GMRES-based refinement (solver Magma_REFINE_IRGMSTRS): as oracle_dsgesv
+ * with each correction (it >= 0; the initial solve is one sgetrs) replaced by
+ * gmres_correction; iter on convergence is the total of the inner iteration
+ * counts. */
+int oracle_dsgesv_gmres(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
+                        int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out)
+{
+    return dsgesv_impl(n, nrhs, A, lda, B, ldb, X, ldx, ipiv, itermax, tol, fallback, iter_out, 1);
+}
+
+static int dsgesv_impl(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
+                       int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out,
+                       int gmres)
 {
     const double eps = 1.1102230246251565e-16;
     double anrm = 0.0;
@@ -246,6 +365,13 @@ int oracle_dsgesv(int n, int nrhs, double *A, int lda, const double *B, int ldb,
         if ((double)rs > anrm) anrm = (double)rs;
     }
     int iter = 0, info = 0, state = 0;   /* 0 active, 1 converged, 2 failed */
+    int inner = 0;
+    float *A32 = NULL;
+    double *beta_prev = (double *)malloc(sizeof(double) * (nrhs > 0 ? nrhs : 1));
+    if (gmres) {
+        A32 = (float *)malloc(sizeof(float) * (size_t)n * n + 4);
+        memcpy(A32, As, sizeof(float) * (size_t)n * n);
+    }
     if (ovf) { iter = -2; state = 2; }
     int sinfo = oracle_sgetrf(n, n, As, n, ipiv);
     if (state == 0 && sinfo > 0) { iter = -3; state = 2; }
@@ -279,14 +405,21 @@ int oracle_dsgesv(int n, int nrhs, double *A, int lda, const double *B, int ldb,
                 if (xs > xrow) xrow = xs;
             }
             if (tol > 0.0) ok = rrow <= tol * (anrm * xrow * (double)n * eps);
-            if (ok) { state = 1; iter = it; break; }
+            if (ok) { state = 1; iter = gmres ? inner : it; break; }
             if (it == itermax) { state = 2; iter = -itermax - 1; break; }
         }
-        for (size_t e = 0; e < (size_t)n * nrhs; e++) Rs[e] = (float)R[e];
-        oracle_sgetrs(0, n, nrhs, As, n, ipiv, Rs, n);
-        for (int c = 0; c < nrhs; c++)
-            for (int i = 0; i < n; i++)
-                X[i + (size_t)c * ldx] = X[i + (size_t)c * ldx] + (double)Rs[i + (size_t)c * n];
+        if (gmres && it >= 0) {
+            int stalled = 0;
+            inner += gmres_correction(n, nrhs, A32, As, ipiv, R, X, ldx, beta_prev, it == 0,
+                                      &stalled);
+            if (stalled) { state = 2; iter = -itermax - 1; break; }
+        } else {
+            for (size_t e = 0; e < (size_t)n * nrhs; e++) Rs[e] = (float)R[e];
+            oracle_sgetrs(0, n, nrhs, As, n, ipiv, Rs, n);
+            for (int c = 0; c < nrhs; c++)
+                for (int i = 0; i < n; i++)
+                    X[i + (size_t)c * ldx] = X[i + (size_t)c * ldx] + (double)Rs[i + (size_t)c * n];
+        }
         for (int c = 0; c < nrhs; c++)
             for (int i = 0; i < n; i++) {
                 double acc = B[i + (size_t)c * ldb];
@@ -301,9 +434,22 @@ int oracle_dsgesv(int n, int nrhs, double *A, int lda, const double *B, int ldb,
             for (int i = 0; i < n; i++) X[i + (size_t)c * ldx] = B[i + (size_t)c * ldb];
         oracle_dgetrs(0, n, nrhs, A, lda, ipiv, X, ldx);
     }
-    free(As); free(Rs); free(R);
+    free(As); free(Rs); free(R); free(A32); free(beta_prev);
     *iter_out = iter;
     return info;
+}
+
+void oracle_dsgesv_gmres_batched(int n, int nrhs, double *A, int lda, long strideA,
+                                 const double *B, int ldb, long strideB, double *X, int ldx,
+                                 long strideX, int *ipiv, long strideP, int *info, int *iter,
+                                 int itermax, double tol, int fallback, int batch, int nthreads)
+{
+    (void)nthreads;
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+    for (int k = 0; k < batch; k++)
+        info[k] = oracle_dsgesv_gmres(n, nrhs, A + k * strideA, lda, B + k * strideB, ldb,
+                                      X + k * strideX, ldx, ipiv + k * strideP, itermax, tol,
+                                      fallback, iter + k);
 }
 
 void oracle_dsgesv_batched(int n, int nrhs, double *A, int lda, long strideA, const double *B,
