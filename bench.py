@@ -268,24 +268,66 @@ class Dsgesv512:
     dominant_class = "ir_residual"
     dominant = "mlu::ir_residual_kernel<4> (FP64 residual R = B - A X)"
 
+    # End to end: the batch goes through the C ABI as two calls, the first on a quarter
+    # of the matrices; all host-to-device copies are queued at once on a copy stream,
+    # so the second chunk arrives while the first is solved, and each chunk's solutions
+    # go back as soon as it is done.  (Measured on GB300: 13.6 ms per step with a
+    # quarter first, 14.1 ms with an eighth, 14.6 ms with a half, 15.5 ms as one call.)
+    E2E_CHUNKS = 2
+    E2E_FIRST = 0.25
+
     def e2e_setup(self, c):
         import torch
+        from magma_gb300.batched import ptr_array
         c["hS"] = c["S"].cpu().pin_memory()
         c["hB"] = c["B"].cpu().pin_memory()
         c["hX"] = torch.empty_like(c["hB"]).pin_memory()
         c["hIter"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
         c["hInfo"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
+        c["copy_stream"] = torch.cuda.Stream()
+        first = int(self.batch * self.E2E_FIRST)
+        c["chunks"] = []
+        for k in range(self.E2E_CHUNKS):
+            sl = slice(0, first) if k == 0 else slice(first, self.batch)
+            c["chunks"].append({"sl": sl, "dS": ptr_array(c["Ss"][0][sl]), "dB": ptr_array(c["B"][sl]),
+                                "dX": ptr_array(c["X"][sl]), "dP": ptr_array(c["ipiv"][sl])})
         h2d = c["hS"].numel() * 8 + c["hB"].numel() * 8
         d2h = c["hX"].numel() * 8 + 8 * self.batch
         return h2d, d2h
 
     def e2e_step(self, c):
-        c["Ss"][0].copy_(c["hS"], non_blocking=True)
-        c["B"].copy_(c["hB"], non_blocking=True)
-        self.step(c, 0)
-        c["hX"].copy_(c["X"], non_blocking=True)
-        c["hIter"].copy_(c["iter"], non_blocking=True)
-        c["hInfo"].copy_(c["info"], non_blocking=True)
+        import torch
+        from magma_gb300.batched import PRECISIONS, SOLVERS
+        main, cs = torch.cuda.current_stream(), c["copy_stream"]
+        cs.wait_stream(main)                      # the previous step is done with the buffers
+        arrived = []
+        with torch.cuda.stream(cs):
+            for ck in c["chunks"]:
+                sl = ck["sl"]
+                c["Ss"][0][sl].copy_(c["hS"][sl], non_blocking=True)
+                c["B"][sl].copy_(c["hB"][sl], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                arrived.append(ev)
+        n, r = self.n, self.nrhs
+        for ck, ev in zip(c["chunks"], arrived):
+            sl = ck["sl"]
+            main.wait_event(ev)
+            rc = c["lib"].magma_dxgesv_gmres_batched_work(
+                PRECISIONS[self.precision], SOLVERS[self.solver], n, r, vp(ck["dS"]), n, vp(ck["dP"]),
+                vp(ck["dB"]), n, vp(ck["dX"]), n, vp(c["info"][sl]), vp(c["iter"][sl]),
+                self.itermax, self.tol, 1, vp(c["work"]), C.byref(c["lwork"]), sl.stop - sl.start,
+                c["q"].handle)
+            if rc != 0:
+                raise RuntimeError(f"magma_dxgesv_gmres_batched_work returned {rc}")
+            done = torch.cuda.Event()
+            done.record(main)
+            with torch.cuda.stream(cs):
+                cs.wait_event(done)
+                c["hX"][sl].copy_(c["X"][sl], non_blocking=True)
+                c["hIter"][sl].copy_(c["iter"][sl], non_blocking=True)
+                c["hInfo"][sl].copy_(c["info"][sl], non_blocking=True)
+        main.wait_stream(cs)                      # the step ends when the results are home
 
     def accuracy(self, c, last):
         X = c["X"].transpose(1, 2)
@@ -1242,6 +1284,7 @@ def run_ours(args, wl):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                "calls_per_step": getattr(wl, "E2E_CHUNKS", 1),
                 "host_cpus": f"{len(cpus)} GPU-local cores" if cpus else "unpinned"},
         "gpu_launches": launches,
         "clocks": clk,
