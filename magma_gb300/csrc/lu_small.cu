@@ -145,6 +145,135 @@ small_gesv_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T *
     if (live && lane == 0) info_array[mat] = info;
 }
 
+// Packed variant for 16 < n <= 32: the matrix of each warp sits row-major in
+// shared memory and rows are interchanged physically.  The pivot search and
+// the column scaling are lane = row as above, but the rank-1 update of step k
+// spreads the (n-1-k)^2 trailing elements over all 32 lanes (element e of the
+// step: row k+1+e/w, column k+1+e%w, w = n-1-k), so no FP64 instruction runs
+// with the lanes of finished rows idle: 344 warp FMAs for the update of a
+// 32 x 32 matrix instead of 496.  Every element receives the same operations
+// in the same order as in small_gesv_kernel.
+constexpr int PK_LD = 33;
+
+template <typename T>
+__host__ __device__ constexpr size_t packed_warp_elems(int nb)
+{
+    return (size_t)32 * PK_LD + (size_t)32 * nb + 32;
+}
+
+template <typename T, int NRHS>
+__global__ void __launch_bounds__(GESV_WARPS * 32)
+small_gesv_packed_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_array, T **dB_array,
+                         int lddb, int *info_array, int batch)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ T s_piv[GESV_WARPS], s_rcp[GESV_WARPS];
+    constexpr int NB = NRHS > 0 ? NRHS : 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int mat = blockIdx.x * GESV_WARPS + warp;
+    const bool live = mat < batch;   // dead warps still take part in the barriers
+    T *sA = reinterpret_cast<T *>(smem_raw) + (size_t)warp * packed_warp_elems<T>(NB);  // [32][PK_LD]
+    T *sB = sA + 32 * PK_LD;                                                           // [32][NB]
+    T *sR = sB + 32 * NB;                                                              // pivot reciprocals
+    const bool row_valid = lane < n;
+    T *A = live ? dA_array[mat] : nullptr;
+#pragma unroll 8
+    for (int j = 0; j < 32; j++)
+        sA[lane * PK_LD + j] = (live && row_valid && j < n) ? A[lane + (size_t)j * ldda] : T(0);
+    T *B = nullptr;
+    if (NRHS > 0) {
+        B = live ? dB_array[mat] : nullptr;
+#pragma unroll
+        for (int c = 0; c < NB; c++)
+            sB[lane * NB + c] = (live && row_valid && c < nrhs) ? B[lane + (size_t)c * lddb] : T(0);
+    }
+    __syncwarp();
+    int info = 0, my_ipiv = 0;
+    for (int k = 0; k < n; k++) {
+        const T v = sA[lane * PK_LD + k];
+        const bool cand = lane >= k && row_valid;
+        unsigned long long key = 0ull;
+        if (cand) {
+            unsigned long long mag = Prec<T>::absbits(v);
+            if (Prec<T>::isnan_(v)) mag = (lane == k) ? 0x7fffffffffffffffull : 0ull;
+            key = mag | 0x8000000000000000ull;
+        }
+        const int p = (int)warp_argmax_key(key, cand ? (unsigned)lane : 0xffffffffu);
+        const T piv = shfl(v, p);
+        const bool nz = Prec<T>::nonzero(piv);
+        if (!nz && info == 0) info = k + 1;
+        if (lane == k) my_ipiv = p + 1;
+        if (p != k) {                                   // whole rows k and p, and the right-hand sides
+            if (row_valid) {
+                const T x = sA[k * PK_LD + lane];
+                sA[k * PK_LD + lane] = sA[p * PK_LD + lane];
+                sA[p * PK_LD + lane] = x;
+            }
+            if (NRHS > 0 && lane < NB) {
+                const T x = sB[k * NB + lane];
+                sB[k * NB + lane] = sB[p * NB + lane];
+                sB[p * NB + lane] = x;
+            }
+        }
+        if (lane == 0) s_piv[warp] = piv;
+        __syncthreads();
+        if (warp == 0 && lane < GESV_WARPS) s_rcp[lane] = T(1) / s_piv[lane];
+        __syncthreads();
+        const T r = s_rcp[warp];
+        if (lane == 0) sR[k] = r;
+        if (lane > k && row_valid && nz) sA[lane * PK_LD + k] = rscale(sA[lane * PK_LD + k], piv, r);
+        __syncwarp();
+        const int w = n - 1 - k;
+        if (w > 0) {
+            const float inv = 1.0f / (float)w;
+            for (int e = lane; e < w * w; e += 32) {
+                int i = __float2int_rz((float)e * inv);
+                int j = e - i * w;
+                if (j < 0) { i--; j += w; } else if (j >= w) { i++; j -= w; }
+                T *dst = sA + (k + 1 + i) * PK_LD + (k + 1 + j);
+                *dst = Prec<T>::fma_(-sA[(k + 1 + i) * PK_LD + k], sA[k * PK_LD + k + 1 + j], *dst);
+            }
+            if (NRHS > 0 && lane > k && row_valid) {
+#pragma unroll
+                for (int c = 0; c < NB; c++)
+                    if (c < nrhs)
+                        sB[lane * NB + c] = Prec<T>::fma_(-sA[lane * PK_LD + k], sB[k * NB + c], sB[lane * NB + c]);
+            }
+        }
+        __syncwarp();
+    }
+    if (NRHS > 0) {
+        // U x = y, lane = row, multiplying by the stored pivot reciprocals
+        for (int t = n - 1; t >= 0; t--) {
+            const T d = sA[t * PK_LD + t], rr = sR[t];
+            T x[NB];
+#pragma unroll
+            for (int c = 0; c < NB; c++) x[c] = rscale(sB[t * NB + c], d, rr);
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c < NB; c++) {
+                if (c < nrhs) {
+                    if (lane == t) sB[t * NB + c] = x[c];
+                    else if (lane < t) sB[lane * NB + c] = Prec<T>::fma_(-sA[lane * PK_LD + t], x[c], sB[lane * NB + c]);
+                }
+            }
+            __syncwarp();
+        }
+    }
+    if (live && row_valid) {
+#pragma unroll 8
+        for (int j = 0; j < 32; j++)
+            if (j < n) A[lane + (size_t)j * ldda] = sA[lane * PK_LD + j];
+        ipiv_array[mat][lane] = my_ipiv;
+        if (NRHS > 0) {
+#pragma unroll
+            for (int c = 0; c < NB; c++)
+                if (c < nrhs) B[lane + (size_t)c * lddb] = sB[lane * NB + c];
+        }
+    }
+    if (live && lane == 0) info_array[mat] = info;
+}
+
 // Solve with existing factors, n <= 32.  NoTrans: lane i holds row i of LU.
 // Trans: lane i holds column i of LU, so that U(t,i) and L(t,i) are static
 // register indices.  RHS columns [blockIdx.y*NRHS, +NRHS).
@@ -260,6 +389,17 @@ template <typename T, int N, int NRHS>
 static void launch_small_gesv(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb,
                               int *info, int batch, cudaStream_t s)
 {
+    if (N == 32) {   // 16 < n <= 32: the packed shared-memory kernel
+        constexpr int NB = NRHS > 0 ? NRHS : 1;
+        const size_t smem = (size_t)GESV_WARPS * packed_warp_elems<T>(NB) * sizeof(T);
+        static size_t dyn = 0;
+        if (!dyn) dyn = mlu_allow_dynamic_smem(small_gesv_packed_kernel<T, NRHS>);
+        if (smem <= dyn) {
+            MLU_LAUNCH(mlu::KC_SMALL_GESV, s, small_gesv_packed_kernel<T, NRHS><<<mlu_ceildiv(batch, GESV_WARPS), GESV_WARPS * 32, smem, s>>>(
+                n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch));
+            return;
+        }
+    }
     MLU_LAUNCH(mlu::KC_SMALL_GESV, s, small_gesv_kernel<T, N, NRHS><<<mlu_ceildiv(batch, GESV_WARPS), GESV_WARPS * 32, 0, s>>>(
         n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch));
 }
