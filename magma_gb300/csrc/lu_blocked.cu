@@ -638,10 +638,18 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
             MLU_LAUNCH(mlu::KC_GEMM, s, band_kernel<<<dim3(bands, nb), BAND_THREADS, band_smem_bytes(), s>>>(
                 m, n, j0, ib, reinterpret_cast<float **>(dAb), ldda, ipb, vs));
         } else if (update && rm > 0 && rn > 0) {
-            const int tiles_m = (rm + BM - 1) / BM, tiles_n = (rn + BN - 1) / BN;
-            MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
-                                                                            (BM / TM) * (BN / TN), 0, s>>>(
-                m, n, j0, ib, dAb, ldda, tiles_m, vs));
+            if (rm <= 32 || rn <= 32) {
+                // a thin trailing block: 32 x 32 tiles, so that no FMA of a
+                // 64 x 64 tile runs on padding (each costs full FP64 issue slots)
+                const int tiles_m = (rm + 31) / 32, tiles_n = (rn + 31) / 32;
+                MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, 32, 32, 2, 2><<<dim3(tiles_m * tiles_n, nb), 256, 0, s>>>(
+                    m, n, j0, ib, dAb, ldda, tiles_m, vs));
+            } else {
+                const int tiles_m = (rm + BM - 1) / BM, tiles_n = (rn + BN - 1) / BN;
+                MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
+                                                                                (BM / TM) * (BN / TN), 0, s>>>(
+                    m, n, j0, ib, dAb, ldda, tiles_m, vs));
+            }
         }
     }
     MLU_CHECK_LAUNCH();

@@ -233,7 +233,13 @@ __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, 
         const T *prow = s_row[buf][gw];
         const T piv = prow[0];
         const bool nz = Prec<T>::nonzero(piv);
-        const T rcp = T(1) / piv;
+        // the reciprocal only in warps that still hold rows: on this part an FP64
+        // division costs the same issue slots in a warp whose lanes do not need it
+        bool any_live = false;
+#pragma unroll
+        for (int r = 0; r < RPT; r++) any_live |= live[r];
+        T rcp = T(0);
+        if (__any_sync(FULL, any_live)) rcp = T(1) / piv;
         if (tid == 0) {
             s_ipiv[k] = (int)gpos;
             if (!nz && info_local == 0) info_local = col0 + k + 1;
