@@ -81,8 +81,10 @@ panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_ar
 // Register-resident panel (pm <= RPT * PANEL_THREADS): one barrier per column;
 // dynamic shared memory panel_regs_smem_bytes<T, RPT>().
 // two CTAs per SM unless the panel rows alone need more than 64 registers
-template <typename T, int RPT, bool NOPIV = false>
-__global__ void __launch_bounds__(PANEL_THREADS, (sizeof(T) * RPT * PANEL_NB / 4 > 64) ? 1 : 2)
+// NT: threads of the CTA (64 or 128 for panels of at most that many rows: fewer
+// warps to synchronise per column, more CTAs per SM).
+template <typename T, int RPT, bool NOPIV = false, int NT = PANEL_THREADS>
+__global__ void __launch_bounds__(NT, (sizeof(T) * RPT * PANEL_NB / 4 > 64) ? 1 : 2)
 panel_regs_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
                   int *info_array, StepSizes vs)
 {
@@ -94,7 +96,7 @@ panel_regs_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ip
         return;
     }
     T *A = dA_array[mat] + j0 + (size_t)j0 * ldda;
-    const int info_local = panel_factor_regs<T, RPT, NOPIV>(m - j0, ib, A, ldda, s_ipiv, j0, smem);
+    const int info_local = panel_factor_regs<T, RPT, NOPIV, NT>(m - j0, ib, A, ldda, s_ipiv, j0, smem);
     if (ipiv_array && tid < ib) ipiv_array[mat][j0 + tid] = j0 + s_ipiv[tid] + 1;
     if (tid == 0) {
         if (j0 == 0) info_array[mat] = info_local;
@@ -542,7 +544,14 @@ template <typename T, bool NOPIV>
 static void launch_panel(int rpt, int m, int n, int j0, int ib, T **dA, int ldda, int **ipiv,
                          int *info, StepSizes vs, int nb, size_t smem, cudaStream_t s)
 {
-    if (rpt == 1)
+    const int pm = m - j0;
+    if (rpt == 1 && pm <= 64)
+        MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 1, NOPIV, 64><<<nb, 64, panel_regs_smem_bytes<T, 1, 64>(), s>>>(
+            m, n, j0, ib, dA, ldda, ipiv, info, vs));
+    else if (rpt == 1 && pm <= 128)
+        MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 1, NOPIV, 128><<<nb, 128, panel_regs_smem_bytes<T, 1, 128>(), s>>>(
+            m, n, j0, ib, dA, ldda, ipiv, info, vs));
+    else if (rpt == 1)
         MLU_LAUNCH(mlu::KC_PANEL, s, panel_regs_kernel<T, 1, NOPIV><<<nb, PANEL_THREADS, smem, s>>>(
             m, n, j0, ib, dA, ldda, ipiv, info, vs));
     else if (rpt == 2)

@@ -143,23 +143,25 @@ __device__ __forceinline__ int panel_factor(int pm, int ib, T *A, int lda, unsig
 // 0; s_ipiv[k] = position (0-based, panel-relative) chosen at step k.
 constexpr int PANEL_REGS_THREADS = 256;
 
-template <typename T, int RPT>
-__host__ __device__ constexpr int panel_regs_ld() { return PANEL_REGS_THREADS * RPT; }
+// NT: the CTA's threads (RPT * NT >= panel rows); 256 unless a shorter panel
+// runs in a smaller CTA.
+template <typename T, int RPT, int NT = PANEL_REGS_THREADS>
+__host__ __device__ constexpr int panel_regs_ld() { return NT * RPT; }
 
-// shared memory that panel_factor_regs<T, RPT> needs from its caller
-template <typename T, int RPT>
+// shared memory that panel_factor_regs<T, RPT, NOPIV, NT> needs from its caller
+template <typename T, int RPT, int NT = PANEL_REGS_THREADS>
 __host__ __device__ constexpr size_t panel_regs_smem_bytes()
 {
-    return (size_t)PANEL_NB * panel_regs_ld<T, RPT>() * sizeof(T) +
-           (size_t)panel_regs_ld<T, RPT>() * sizeof(int);
+    return (size_t)PANEL_NB * panel_regs_ld<T, RPT, NT>() * sizeof(T) +
+           (size_t)panel_regs_ld<T, RPT, NT>() * sizeof(int);
 }
 
-template <typename T, int RPT, bool NOPIV = false>
+template <typename T, int RPT, bool NOPIV = false, int NT = PANEL_REGS_THREADS>
 __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, int *s_ipiv,
                                                  int col0, unsigned char *smem)
 {
-    constexpr int NW = PANEL_REGS_THREADS / 32;
-    constexpr int LDP = panel_regs_ld<T, RPT>();
+    constexpr int NW = NT / 32;
+    constexpr int LDP = panel_regs_ld<T, RPT, NT>();
     __shared__ unsigned s_hi[2][NW], s_lo[2][NW], s_pos[2][NW];
     __shared__ __align__(16) T s_row[2][NW][PANEL_NB];
     T *sP = reinterpret_cast<T *>(smem);
@@ -171,7 +173,7 @@ __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, 
     bool live[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; r++) {
-        const int i = tid + r * PANEL_REGS_THREADS;
+        const int i = tid + r * NT;
         live[r] = i < pm;
         pos[r] = i;
 #pragma unroll
@@ -247,7 +249,7 @@ __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, 
 #pragma unroll
         for (int r = 0; r < RPT; r++) {
             if (!live[r]) continue;
-            const int slot = tid + r * PANEL_REGS_THREADS;
+            const int slot = tid + r * NT;
             // interchange of positions k and gpos
             if (pos[r] == (int)gpos) pos[r] = k;
             else if (pos[r] == k) pos[r] = (int)gpos;
@@ -268,14 +270,14 @@ __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, 
     // write back in pivoted order: position -> slot map, then coalesced rows
 #pragma unroll
     for (int r = 0; r < RPT; r++) {
-        const int slot = tid + r * PANEL_REGS_THREADS;
+        const int slot = tid + r * NT;
         if (slot < pm) s_slot[pos[r]] = slot;
     }
     __syncthreads();
     for (int j = 0; j < ib; j++) {
 #pragma unroll
         for (int r = 0; r < RPT; r++) {
-            const int p = tid + r * PANEL_REGS_THREADS;
+            const int p = tid + r * NT;
             if (p < pm) A[p + (size_t)j * lda] = sP[(size_t)j * LDP + s_slot[p]];
         }
     }
