@@ -211,6 +211,15 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant_
         const int cbase = j0 + ib + tn * TC_N;
 #pragma unroll 1
         for (int cc = 0; cc < TC_N; cc += 16) {
+            // this chunk's 16 elements of A22 first: all loads in flight together and
+            // overlapping the TMEM read (element by element, each load would wait for
+            // the previous store)
+            float a[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int c = cbase + cc + j;
+                a[j] = (r < m && c < n) ? A[r + (size_t)c * ldda] : 0.f;
+            }
             uint32_t v[16];
             asm volatile(
                 "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
@@ -224,10 +233,7 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant_
 #pragma unroll
                 for (int j = 0; j < 16; j++) {
                     const int c = cbase + cc + j;
-                    if (c < n) {
-                        float *p = A + r + (size_t)c * ldda;
-                        *p = *p + __uint_as_float(v[j]);
-                    }
+                    if (c < n) A[r + (size_t)c * ldda] = a[j] + __uint_as_float(v[j]);
                 }
             }
         }
