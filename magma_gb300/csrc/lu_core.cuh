@@ -460,6 +460,13 @@ __device__ __forceinline__ void gemm_tile(T *A, int lda, int m, int n, int j0, i
         }
     }
     __syncthreads();
+    // Nothing of this thread's block is stored when its columns (or rows) lie past
+    // the matrix, or (SYRK) the block lies above the diagonal: it leaves now (no
+    // barrier follows).  A warp's lanes share their columns, so at the right edge of
+    // the trailing matrix whole warps issue no FMAs, which on this part's FP64 pipe
+    // cost their issue slots whether or not any lane keeps the result.
+    if (c0 + tc * TN >= n || r0 + tr * TM >= m) return;
+    if (SYRK && r0 + tr * TM + TM - 1 < c0 + tc * TN) return;
     int k = 0;
     // four k at a time: each thread's U entries for 4 consecutive k are contiguous
     for (; k + 4 <= ib; k += 4) {
