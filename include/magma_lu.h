@@ -478,6 +478,34 @@ magma_int_t magma_dxgesv_gmres_batched_work(magma_int_t precision, magma_int_t s
                                             void *work, size_t *lwork,
                                             magma_int_t batchCount, magma_queue_t queue);
 
+/* Batched form of magma_dsposv_gpu (src/zcposv_gpu.cpp:134, declared as
+ * magma_zcposv_gpu in include/magma_zc.h:69): for symmetric positive definite
+ * A (lower triangle referenced), FP32 Cholesky of float(A) and FP64 refinement
+ * (FP64 residual, update and stopping rule, FP32 L L^T corrections); ITER
+ * codes, tol, fallback and the workspace query as magma_dsgesv_batched_work
+ * (-3: the FP32 Cholesky met a non-positive pivot).  With fallback, matrices
+ * that did not converge are solved by magma_dposv_batched in FP64 (A then
+ * holds their FP64 Cholesky factor, info its result).  MagmaUpper returns -1.
+ * Errors: -1 uplo, -2 n, -3 nrhs (> 16), -5 ldda, -7 lddb, -9 lddx,
+ * -12 itermax. */
+magma_int_t magma_dsposv_batched_work(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs,
+                                      double **dA_array, magma_int_t ldda,
+                                      double **dB_array, magma_int_t lddb,
+                                      double **dX_array, magma_int_t lddx,
+                                      magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                      magma_int_t itermax, double tol, magma_int_t fallback,
+                                      void *work, size_t *lwork,
+                                      magma_int_t batchCount, magma_queue_t queue);
+/* magma_dsposv_batched_work with itermax 30, the default stopping rule, the
+ * fallback, and workspace owned by the queue (allocated, after a
+ * synchronisation, when too small). */
+magma_int_t magma_dsposv_batched(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs,
+                                 double **dA_array, magma_int_t ldda,
+                                 double **dB_array, magma_int_t lddb,
+                                 double **dX_array, magma_int_t lddx,
+                                 magma_int_t *dinfo_array, magma_int_t *diter_array,
+                                 magma_int_t batchCount, magma_queue_t queue);
+
 /* No counterpart in the reference: the batched refinement of
  * magma_dxgesv_batched_work for a variable-size batch.  n[k], nrhs[k], ldda[k],
  * lddb[k] and lddx[k] are device arrays; max_n and max_nrhs (<= 16) are their

@@ -6,14 +6,14 @@ ctypes binding (`lib`), tensor-level wrappers (`batched`) and seeded input
 generators (`testing`).
 """
 from . import lib  # noqa: F401
-from .batched import (Queue, VBatch, autotune_vbatched, colmajor, dsgesv_batched,  # noqa: F401
+from .batched import (Queue, VBatch, autotune_vbatched, colmajor, dsgesv_batched, dsposv_batched,  # noqa: F401
                       dsgesv_adjoint_batched, dxgesv_adjoint_vbatched, dxgesv_vbatched,
                       dsgesv_workspace_bytes, from_colmajor, gesv_batched, gesv_vbatched,
                       getrf_batched, getrs_batched, ptr_array, set_vbatched_tuning,
                       vbatched_tuning)
 
 __all__ = ["lib", "Queue", "colmajor", "from_colmajor", "ptr_array", "getrf_batched",
-           "getrs_batched", "gesv_batched", "dsgesv_batched", "dsgesv_workspace_bytes",
+           "getrs_batched", "gesv_batched", "dsgesv_batched", "dsposv_batched", "dsgesv_workspace_bytes",
            "VBatch", "gesv_vbatched", "vbatched_tuning", "set_vbatched_tuning",
            "autotune_vbatched", "dxgesv_vbatched", "dsgesv_adjoint_batched",
            "dxgesv_adjoint_vbatched"]

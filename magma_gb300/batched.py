@@ -211,6 +211,36 @@ def dsgesv_batched(S: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = No
 SOLVERS = {"ir": 920, "gmres": 922}
 
 
+def dsposv_batched(S: torch.Tensor, B: torch.Tensor, X: torch.Tensor | None = None,
+                   itermax: int = 30, tol: float = 0.0, fallback: bool = True,
+                   queue: Queue | None = None):
+    """Batched FP32-Cholesky / FP64-refinement SPD solve (magma_dsposv_batched_work,
+    lower triangle).  S, B FP64 column-major storage; S is left unchanged unless a
+    matrix falls back to FP64.  Returns (X, info, iters)."""
+    _check_storage(S, "S")
+    _check_storage(B, "B")
+    b, n, ld = S.shape
+    nrhs, ldb = B.shape[1], B.shape[2]
+    X = torch.empty_like(B) if X is None else X
+    info = torch.empty((b,), dtype=torch.int32, device=S.device)
+    iters = torch.empty((b,), dtype=torch.int32, device=S.device)
+    q = queue or Queue.current(S.device)
+    lib = _L.load()
+    lw = C.c_size_t(0)
+    rc = lib.magma_dsposv_batched_work(122, n, nrhs, None, max(ld, 1), None, max(ldb, 1), None,
+                                       max(X.shape[2], 1), None, None, itermax, float(tol), 0,
+                                       None, C.byref(lw), b, None)
+    _check(rc, "magma_dsposv_batched_work(query)")
+    work = torch.empty((max(int(lw.value), 1),), dtype=torch.uint8, device=S.device)
+    lw = C.c_size_t(work.numel())
+    dA, dB, dX = ptr_array(S), ptr_array(B), ptr_array(X)
+    rc = lib.magma_dsposv_batched_work(122, n, nrhs, _vp(dA), ld, _vp(dB), ldb, _vp(dX),
+                                       X.shape[2], _vp(info), _vp(iters), itermax, float(tol),
+                                       1 if fallback else 0, _vp(work), C.byref(lw), b, q.handle)
+    _check(rc, "magma_dsposv_batched_work")
+    return X, info, iters
+
+
 def dsgesv_workspace_bytes(n: int, nrhs: int, batch: int, precision: str = "fp32",
                            solver: str = "ir") -> int:
     lib = _L.load()

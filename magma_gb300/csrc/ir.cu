@@ -27,11 +27,14 @@
 #include "trace.cuh"
 #include "convert.cuh"
 #include "solve_core.cuh"
+#include "chol_core.cuh"
 
 namespace mlu {
 template <typename T>
 magma_int_t blocked_getrf(int m, int n, T **dA, int ldda, int **ipiv, int *info, int batch,
                           magma_queue_t q);
+template <typename T>
+magma_int_t chol_factor(int n, T **dA, int lda, int *info, int batch, magma_queue_t q);
 template <typename T>
 magma_int_t small_gesv(int n, int nrhs, T **dA, int ldda, int **ipiv, T **dB, int lddb, int *info,
                        int batch, magma_queue_t q);
@@ -264,7 +267,9 @@ __device__ __forceinline__ bool ir_converged(const unsigned long long *st, int p
 // factors.  One CTA per (matrix, group of NR right-hand sides).
 // Four CTAs per SM (64 registers a thread): the solves are latency-bound, so a
 // whole batch of 512 matrices resident at once beats more registers per thread.
-template <int NR, bool TRANS>
+// SPD: the factors are the FP32 Cholesky factor L (lower), the correction is
+// L L^T d = r (no interchanges, no scaling).
+template <int NR, bool TRANS, bool SPD = false>
 __global__ void __launch_bounds__(256, 4)
 ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double **dX_array,
                 const double *R, unsigned long long *stats, int *iter, const int *info, int it,
@@ -299,8 +304,13 @@ ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double
     const int c0 = blockIdx.x * NR;
     const int nr = min(NR, nrhs - c0);
     const double *Rm = R + ((size_t)mat * sh.nrhs + c0) * sh.n;
-    const int *pm = perm + (size_t)mat * sh.n;
-    if (!TRANS) {
+    const int *pm = SPD ? nullptr : perm + (size_t)mat * sh.n;
+    if (SPD) {
+        for (int e = tid; e < NR * n; e += blockDim.x) {
+            const int c = e / n, i = e % n;
+            sB[c * n + i] = __double2float_rn(c < nr ? Rm[i + (size_t)c * sh.n] : 0.0);
+        }
+    } else if (!TRANS) {
         // row interchanges applied while loading: sB[i] = R[perm[i]]
         for (int e = tid; e < NR * n; e += blockDim.x) {
             const int c = e / n, i = e % n;
@@ -315,13 +325,15 @@ ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double
         }
     }
     __syncthreads();
-    solve_smem<float, TRANS, NR>(n, dAs_array[mat], ldas, nullptr, sB, nr);
+    if (SPD) chol_solve_smem<float, NR>(n, dAs_array[mat], ldas, sB);
+    else solve_smem<float, TRANS, NR>(n, dAs_array[mat], ldas, nullptr, sB, nr);
+    __syncthreads();
     double *X = dX_array[mat] + (size_t)c0 * lddx;
     for (int e = tid; e < nr * n; e += blockDim.x) {
         const int c = e / n, i = e % n;
         const double d = (double)sB[c * n + i];
         // A^T: the interchanges undone on the way out, x[perm[i]] += w[i]
-        const int r = TRANS ? pm[i] : i;
+        const int r = (TRANS && !SPD) ? pm[i] : i;
         X[r + (size_t)c * lddx] = X[r + (size_t)c * lddx] +
                                   (colscale ? d * colscale[(size_t)mat * sh.n + i] : d);
     }
@@ -826,7 +838,7 @@ __global__ void ir_compact_kernel(IrShape sh, double **dA_array, int **ipiv_arra
     if (threadIdx.x == 0) {
         slot = atomicAdd(counter, 1);
         cA[slot] = dA_array[mat];
-        cP[slot] = ipiv_array[mat];
+        cP[slot] = ipiv_array ? ipiv_array[mat] : nullptr;   // no pivots: the SPD form
         cX[slot] = dX_array[mat];
         cidx[slot] = mat;
         if (csize) {          // variable sizes: n, nrhs, ldda, lddx of the compacted batch
@@ -950,11 +962,20 @@ template <bool TRANS>
 static void correction_solve(const IrShape &sh, float **As_array, int ldas, const int *perm,
                              double **dX, const double *R, unsigned long long *stats, int *iter,
                              const int *info, int it, double tol, const double *rsc,
-                             const double *csc, int batch, cudaStream_t s)
+                             const double *csc, int batch, cudaStream_t s, bool spd = false)
 {
     const int snr = sh.nrhs <= 4 ? 4 : IR_SOLVE_NR;   // right-hand sides per CTA
     const size_t ssmem = (size_t)snr * sh.n * sizeof(float);
     const dim3 grid(mlu_ceildiv(sh.nrhs, snr), batch);
+    if (spd) {
+        if (snr == 4)
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4, false, true><<<grid, 256, ssmem, s>>>(
+                sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, nullptr, nullptr));
+        else
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<IR_SOLVE_NR, false, true><<<grid, 256, ssmem, s>>>(
+                sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, nullptr, nullptr));
+        return;
+    }
     if (snr == 4)
         MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4, TRANS><<<grid, 256, ssmem, s>>>(
             sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, rsc, csc));
@@ -976,10 +997,12 @@ static size_t solve_dyn_max()
 {
     static size_t v = 0;
     if (!v)
-        v = min(min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false>),
-                    mlu_allow_dynamic_smem(ir_solve_kernel<4, false>)),
-                min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, true>),
-                    mlu_allow_dynamic_smem(ir_solve_kernel<4, true>)));
+        v = min(min(min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false>),
+                        mlu_allow_dynamic_smem(ir_solve_kernel<4, false>)),
+                    min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, true>),
+                        mlu_allow_dynamic_smem(ir_solve_kernel<4, true>))),
+                min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false, true>),
+                    mlu_allow_dynamic_smem(ir_solve_kernel<4, false, true>)));
     return v;
 }
 
@@ -997,11 +1020,12 @@ static magma_int_t
 ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array,
        double **dB_array, double **dX_array, magma_int_t *dinfo_array, magma_int_t *diter_array,
        magma_int_t itermax, double tol, magma_int_t fallback, void *work, size_t *lwork,
-       magma_int_t batchCount, magma_queue_t queue, int solver = 920)
+       magma_int_t batchCount, magma_queue_t queue, int solver = 920, bool spd = false)
 {
     const bool vb = sh.n_arr != nullptr;
     const int n = sh.n, nrhs = sh.nrhs;
     const bool gm = solver == 922;
+    if (spd && (vb || gm || prec != 900)) return MAGMA_ERR_NOT_SUPPORTED;
     const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0), prec, vb, solver);
     if (work == nullptr) {          // workspace query
         *lwork = L.total;
@@ -1037,7 +1061,9 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
         MLU_LAUNCH(mlu::KC_IR_INIT, s, ir_colscale_kernel<<<dim3((n + 127) / 128, batchCount), 128, 0, s>>>(
             n, dA_array, sh.lda, As_array, L.ldas, rsc, csc));
     magma_int_t rc;
-    if (vb) {
+    if (spd) {
+        rc = chol_factor<float>(n, As_array, L.ldas, dinfo_array, batchCount, queue);
+    } else if (vb) {
         rc = vb_run<float>(sh.n_arr, sh.n_arr, nullptr, n, n, 0, As_array, ldas_arr, dipiv_array,
                            nullptr, nullptr, dinfo_array, w + L.vbw, batchCount, queue, nullptr);
     } else if (prec == 900) {
@@ -1050,11 +1076,12 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
     }
     if (rc != 0) return rc;
     int *perm = (int *)(w + L.perm);
-    MLU_LAUNCH(mlu::KC_OTHER, s, ir_perm_kernel<<<batchCount, 256, (size_t)n * sizeof(int), s>>>(
-        sh, dipiv_array, perm));
+    if (!spd)
+        MLU_LAUNCH(mlu::KC_OTHER, s, ir_perm_kernel<<<batchCount, 256, (size_t)n * sizeof(int), s>>>(
+            sh, dipiv_array, perm));
     auto solve = [&](int it) {
         correction_solve<false>(sh, As_array, L.ldas, perm, dX_array, R, stats, diter_array,
-                                dinfo_array, it, tol, rsc, csc, batchCount, s);
+                                dinfo_array, it, tol, rsc, csc, batchCount, s, spd);
     };
     float *A32 = gm ? (float *)(w + L.gm_a32) : nullptr;
     float *Vk = gm ? (float *)(w + L.gm_v) : nullptr;
@@ -1105,7 +1132,9 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
     MLU_LAUNCH(mlu::KC_OTHER, s, ir_compact_kernel<<<batchCount, 256, 0, s>>>(
         sh, dA_array, dipiv_array, dB_array, dX_array, stats, batchCount, count + 1, cA, cP, cX,
         cidx, csize));
-    if (vb)
+    if (spd)
+        rc = magma_dposv_batched(MagmaLower, n, nrhs, cA, sh.lda, cX, sh.ldx, cinfo, failed, queue);
+    else if (vb)
         rc = vb_run<double>(csize, csize, csize + batchCount, n, n, nrhs, cA, csize + 2 * batchCount,
                             cP, cX, csize + 3 * batchCount, cinfo, w + L.vbw, failed, queue,
                             nullptr);
@@ -1318,6 +1347,63 @@ magma_dxgesv_gmres_batched_work(magma_int_t precision, magma_int_t solver_type, 
     return ir_driver(__func__, 2, precision, n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb,
                      dX_array, lddx, dinfo_array, diter_array, itermax, tol, fallback, work, lwork,
                      batchCount, queue, (int)solver_type);
+}
+
+// Batched form of magma_dsposv_gpu (src/zcposv_gpu.cpp:134-360): FP32 Cholesky of float(A)
+// (lower), FP64 residual, update and stopping rule with FP32 L L^T corrections; the
+// iteration codes of magma_dsgesv_batched_work (-3: the FP32 Cholesky found a
+// non-positive pivot), and with `fallback` an FP64 magma_dposv_batched of the matrices
+// that did not converge (A then holds their FP64 factor).
+extern "C" magma_int_t
+magma_dsposv_batched_work(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs, double **dA_array,
+                          magma_int_t ldda, double **dB_array, magma_int_t lddb,
+                          double **dX_array, magma_int_t lddx, magma_int_t *dinfo_array,
+                          magma_int_t *diter_array, magma_int_t itermax, double tol,
+                          magma_int_t fallback, void *work, size_t *lwork,
+                          magma_int_t batchCount, magma_queue_t queue)
+{
+    magma_int_t info = 0;
+    if (uplo != MagmaLower) info = -1;           // MagmaUpper: not provided, as the batched potrf
+    else if (n < 0) info = -2;
+    else if (nrhs < 0 || nrhs > IR_NRHS_MAX) info = -3;
+    else if (ldda < mlu_max(1, n)) info = -5;
+    else if (lddb < mlu_max(1, n)) info = -7;
+    else if (lddx < mlu_max(1, n)) info = -9;
+    else if (itermax < 0) info = -12;
+    if (info != 0) {
+        magma_xerbla(__func__, -info);
+        return info;
+    }
+    const IrShape sh = {n, nrhs, ldda, lddb, lddx, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return ir_run(900, sh, dA_array, nullptr, dB_array, dX_array, dinfo_array, diter_array,
+                  itermax, tol, fallback, work, lwork, batchCount, queue, 920, true);
+}
+
+extern "C" magma_int_t
+magma_dsposv_batched(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs, double **dA_array,
+                     magma_int_t ldda, double **dB_array, magma_int_t lddb, double **dX_array,
+                     magma_int_t lddx, magma_int_t *dinfo_array, magma_int_t *diter_array,
+                     magma_int_t batchCount, magma_queue_t queue)
+{
+    size_t lwork = 0;
+    magma_int_t rc = magma_dsposv_batched_work(uplo, n, nrhs, dA_array, ldda, dB_array, lddb,
+                                               dX_array, lddx, dinfo_array, diter_array, 30, 0.0,
+                                               1, nullptr, &lwork, batchCount, queue);
+    if (rc != 0) return rc;
+    if (n == 0 || nrhs == 0 || batchCount <= 0) return 0;
+    if (queue->work_bytes < lwork) {
+        if (queue->work) {
+            cudaStreamSynchronize(queue->stream);
+            cudaFree(queue->work);
+        }
+        queue->work = nullptr;
+        queue->work_bytes = 0;
+        if (cudaMalloc(&queue->work, lwork) != cudaSuccess) return MAGMA_ERR_DEVICE_ALLOC;
+        queue->work_bytes = lwork;
+    }
+    return magma_dsposv_batched_work(uplo, n, nrhs, dA_array, ldda, dB_array, lddb, dX_array,
+                                     lddx, dinfo_array, diter_array, 30, 0.0, 1, queue->work,
+                                     &lwork, batchCount, queue);
 }
 
 extern "C" magma_int_t

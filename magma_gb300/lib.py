@@ -131,6 +131,11 @@ for _p in "ds":
 _PROTOS["magma_dxgesv_gmres_batched_work"] = ([c_int, c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_ptr,
                                                c_int, c_ptr, c_int, c_ptr, c_ptr, c_int, C.c_double,
                                                c_int, c_ptr, c_ptr, c_int, c_ptr], c_int)
+_PROTOS["magma_dsposv_batched_work"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, c_int,
+                                         c_ptr, c_ptr, c_int, C.c_double, c_int, c_ptr, c_ptr,
+                                         c_int, c_ptr], c_int)
+_PROTOS["magma_dsposv_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, c_int,
+                                    c_ptr, c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
 _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],

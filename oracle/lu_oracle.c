@@ -325,12 +325,40 @@ done:
 
 static int dsgesv_impl(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
                        int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out,
-                       int gmres);
+                       int gmres, int spd);
+int oracle_spotrf(int n, float *A, int lda);
+void oracle_spotrs(int n, int nrhs, const float *L, int lda, float *B, int ldb);
+int oracle_dpotrf(int n, double *A, int lda);
+void oracle_dpotrs(int n, int nrhs, const double *L, int lda, double *B, int ldb);
+
+/* The mixed-precision SPD refinement (the GPU's magma_dsposv_batched_work; the
+ * reference's magma_dsposv_gpu, src/zcposv_gpu.cpp:134): as oracle_dsgesv with
+ * the FP32 Cholesky (oracle_spotrf, lower; info > 0: iter -3) in place of the
+ * FP32 LU, corrections by oracle_spotrs, and the FP64 fallback oracle_dpotrf +
+ * oracle_dpotrs (the solve runs whatever the factorisation's info). */
+int oracle_dsposv(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
+                  int ldx, int itermax, double tol, int fallback, int *iter_out)
+{
+    return dsgesv_impl(n, nrhs, A, lda, B, ldb, X, ldx, NULL, itermax, tol, fallback, iter_out,
+                       0, 1);
+}
+
+void oracle_dsposv_batched(int n, int nrhs, double *A, int lda, long strideA, const double *B,
+                           int ldb, long strideB, double *X, int ldx, long strideX, int *info,
+                           int *iter, int itermax, double tol, int fallback, int batch,
+                           int nthreads)
+{
+    (void)nthreads;
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+    for (int k = 0; k < batch; k++)
+        info[k] = oracle_dsposv(n, nrhs, A + k * strideA, lda, B + k * strideB, ldb,
+                                X + k * strideX, ldx, itermax, tol, fallback, iter + k);
+}
 
 int oracle_dsgesv(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
                   int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out)
 {
-    return dsgesv_impl(n, nrhs, A, lda, B, ldb, X, ldx, ipiv, itermax, tol, fallback, iter_out, 0);
+    return dsgesv_impl(n, nrhs, A, lda, B, ldb, X, ldx, ipiv, itermax, tol, fallback, iter_out, 0, 0);
 }
 
 /* The GMRES-based refinement (solver Magma_REFINE_IRGMSTRS): as oracle_dsgesv
@@ -340,12 +368,12 @@ int oracle_dsgesv(int n, int nrhs, double *A, int lda, const double *B, int ldb,
 int oracle_dsgesv_gmres(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
                         int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out)
 {
-    return dsgesv_impl(n, nrhs, A, lda, B, ldb, X, ldx, ipiv, itermax, tol, fallback, iter_out, 1);
+    return dsgesv_impl(n, nrhs, A, lda, B, ldb, X, ldx, ipiv, itermax, tol, fallback, iter_out, 1, 0);
 }
 
 static int dsgesv_impl(int n, int nrhs, double *A, int lda, const double *B, int ldb, double *X,
                        int ldx, int *ipiv, int itermax, double tol, int fallback, int *iter_out,
-                       int gmres)
+                       int gmres, int spd)
 {
     const double eps = 1.1102230246251565e-16;
     double anrm = 0.0;
@@ -373,7 +401,7 @@ static int dsgesv_impl(int n, int nrhs, double *A, int lda, const double *B, int
         memcpy(A32, As, sizeof(float) * (size_t)n * n);
     }
     if (ovf) { iter = -2; state = 2; }
-    int sinfo = oracle_sgetrf(n, n, As, n, ipiv);
+    int sinfo = spd ? oracle_spotrf(n, As, n) : oracle_sgetrf(n, n, As, n, ipiv);
     if (state == 0 && sinfo > 0) { iter = -3; state = 2; }
     for (int c = 0; c < nrhs; c++)
         for (int i = 0; i < n; i++) {
@@ -415,7 +443,8 @@ static int dsgesv_impl(int n, int nrhs, double *A, int lda, const double *B, int
             if (stalled) { state = 2; iter = -itermax - 1; break; }
         } else {
             for (size_t e = 0; e < (size_t)n * nrhs; e++) Rs[e] = (float)R[e];
-            oracle_sgetrs(0, n, nrhs, As, n, ipiv, Rs, n);
+            if (spd) oracle_spotrs(n, nrhs, As, n, Rs, n);
+            else oracle_sgetrs(0, n, nrhs, As, n, ipiv, Rs, n);
             for (int c = 0; c < nrhs; c++)
                 for (int i = 0; i < n; i++)
                     X[i + (size_t)c * ldx] = X[i + (size_t)c * ldx] + (double)Rs[i + (size_t)c * n];
@@ -429,10 +458,11 @@ static int dsgesv_impl(int n, int nrhs, double *A, int lda, const double *B, int
             }
     }
     if (state == 2 && fallback) {
-        info = oracle_dgetrf(n, n, A, lda, ipiv);
+        info = spd ? oracle_dpotrf(n, A, lda) : oracle_dgetrf(n, n, A, lda, ipiv);
         for (int c = 0; c < nrhs; c++)
             for (int i = 0; i < n; i++) X[i + (size_t)c * ldx] = B[i + (size_t)c * ldb];
-        oracle_dgetrs(0, n, nrhs, A, lda, ipiv, X, ldx);
+        if (spd) oracle_dpotrs(n, nrhs, A, lda, X, ldx);
+        else oracle_dgetrs(0, n, nrhs, A, lda, ipiv, X, ldx);
     }
     free(As); free(Rs); free(R); free(A32); free(beta_prev);
     *iter_out = iter;

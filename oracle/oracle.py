@@ -237,6 +237,25 @@ def dsgesv_gmres_batched(A, B, itermax=30, tol=0.0, fallback=True, nthreads=None
     return X, ipiv, info, iters
 
 
+def dsposv_batched(A, B, itermax=30, tol=0.0, fallback=True, nthreads=None):
+    """Mixed-precision SPD refinement restatement (oracle_dsposv): FP32 Cholesky
+    (lower), FP64 refinement, FP64 posv fallback.  Returns (X, info, iters)."""
+    lib = load()
+    assert A.dtype == np.float64 and B.dtype == np.float64
+    b, n, ld = A.shape
+    nrhs, ldb = B.shape[1], B.shape[2]
+    X = np.zeros_like(B)
+    info = np.zeros((b,), dtype=np.int32)
+    iters = np.zeros((b,), dtype=np.int32)
+    fn = lib.oracle_dsposv_batched
+    fn.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_int, C.c_long,
+                   C.c_void_p, C.c_int, C.c_long, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                   C.c_int, C.c_int, C.c_int]
+    fn(n, nrhs, _p(A), ld, n * ld, _p(B), ldb, nrhs * ldb, _p(X), ldb, nrhs * ldb, _p(info),
+       _p(iters), itermax, float(tol), 1 if fallback else 0, b, _threads(nthreads))
+    return X, info, iters
+
+
 def getrf_nopiv(A2, m=None):
     """LU without pivoting of one matrix, (ncols, ld) storage, in place.  Returns info."""
     lib = load()
