@@ -137,3 +137,23 @@ def test_potrf_failure_info_vs_lapack(n, bad):
     S = np.ascontiguousarray(_spd(rng, n).T)
     S[0, 0] = np.nan
     assert oracle.potrf(S) == 1
+
+
+def test_oracle_dsposv_refines_and_falls_back():
+    """The SPD refinement restatement: converges for kappa up to 1e6 (FP32 Cholesky +
+    FP64 refinement), and an FP32 Cholesky failure (kappa 1e12) goes to the FP64
+    posv with iter -3 and an accurate solution."""
+    from tests.util import from_storage, scaled_residual, to_storage
+    rng = np.random.default_rng(21)
+    n = 80
+    A = np.empty((4, n, n))
+    for k, kap in enumerate([1e2, 1e4, 1e6, 1e12]):
+        Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        M = (Q * np.geomspace(1.0, 1.0 / kap, n)) @ Q.T
+        A[k] = (M + M.T) / 2
+    B = rng.uniform(-1, 1, (4, n, 3))
+    X, info, iters = oracle.dsposv_batched(to_storage(A), to_storage(B))
+    assert np.all(info == 0)
+    assert np.all(iters[:3] >= 1) and iters[0] <= iters[2], iters
+    assert iters[3] == -3, iters
+    assert scaled_residual(A, from_storage(X, n), B).max() <= 30
