@@ -82,3 +82,28 @@ def test_nopiv_rectangular_and_errors(cuda):
     assert lib.magma_dgetrf_nopiv_batched(4, 4, None, 3, None, 1, q) == -4
     assert lib.magma_dgesv_nopiv_batched(4, 1, None, 4, None, 3, None, 1, q) == -6
     assert lib.magma_dgetrs_nopiv_batched(111, 4, 1, None, 3, None, 4, None, 1, q) == -5
+
+
+def test_nopiv_band_path(cuda):
+    """A batch large enough for the FP32 band kernel (no interchanges to resolve)."""
+    n, batch, nrhs = 100, 320, 2
+    rng = np.random.default_rng(31)
+    S = rng.uniform(-1, 1, (batch, n, n)).astype(np.float32)
+    S[:, np.arange(n), np.arange(n)] += 4.0
+    B = rng.uniform(-1, 1, (batch, nrhs, n)).astype(np.float32)
+    dS, dB = torch.from_numpy(S.copy()).to(cuda), torch.from_numpy(B.copy()).to(cuda)
+    info = torch.full((batch,), -9, dtype=torch.int32, device=cuda)
+    lib = L.load()
+    q = Queue.current(cuda).handle
+    pS, pB = ptr_array(dS), ptr_array(dB)
+    assert lib.magma_sgesv_nopiv_batched(n, nrhs, _vp(pS), n, _vp(pB), n, _vp(info), batch, q) == 0
+    torch.cuda.synchronize()
+    gS, gB = dS.cpu().numpy(), dB.cpu().numpy()
+    assert (info.cpu().numpy() == 0).all()
+    ident = np.arange(1, n + 1, dtype=np.int32)
+    for k in range(0, batch, 37):
+        rS, rB = S[k].copy(), B[k].copy()
+        assert oracle.getrf_nopiv(rS) == 0
+        oracle.sgetrs(rS, ident, rB)
+        assert np.array_equal(gS[k], rS), k
+        assert np.array_equal(gB[k], rB), k
