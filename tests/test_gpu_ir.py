@@ -196,6 +196,26 @@ def test_dxgesv_vbatched_matches_oracle(cuda, tol):
     assert (it < 0).any() and (it >= 0).any()
 
 
+def test_dxgesv_vbatched_band_path_matches_oracle(cuda):
+    """Variable-size refinement with matrices above 256 and a large batch: the FP32
+    factorisation runs through the per-step kernels with per-matrix sizes and the band
+    kernel; bit-identical to the oracle matrix by matrix."""
+    ns, rs, As, Bs = _vb_case(5, 320, 400, 4)
+    A = mg.VBatch([a.shape for a in As], ns, torch.float64, cuda).load(As)
+    B = mg.VBatch([b.shape for b in Bs], ns, torch.float64, cuda).load(Bs)
+    X, ipiv, offs, info, iters, _ = mg.dxgesv_vbatched(A, B, tol=30.0)
+    torch.cuda.synchronize()
+    rA = [a.copy() for a in As]
+    rX, rp, rinfo, riters = oracle.dsgesv_vbatched(rA, Bs, tol=30.0)
+    assert max(ns) > 256
+    assert np.array_equal(iters.cpu().numpy(), riters)
+    assert np.array_equal(info.cpu().numpy(), rinfo)
+    P = ipiv.cpu().numpy()
+    for k, n in enumerate(ns):
+        assert np.array_equal(P[offs[k]:offs[k] + n], rp[k]), k
+        assert np.array_equal(X.view(k).cpu().numpy(), rX[k], equal_nan=True), k
+
+
 def test_dsgesv_adjoint_matches_oracle(cuda):
     """Adjoint of the refinement solve: GB = A^{-T} G refined with the forward's FP32
     factors, GA = -GB X^T; bit-identical to the oracle, including matrices whose forward
