@@ -157,3 +157,25 @@ def test_oracle_dsposv_refines_and_falls_back():
     assert np.all(iters[:3] >= 1) and iters[0] <= iters[2], iters
     assert iters[3] == -3, iters
     assert scaled_residual(A, from_storage(X, n), B).max() <= 30
+
+
+@pytest.mark.parametrize("n", [1, 7, 33, 100])
+def test_oracle_getri_and_adjoint_vs_numpy(n):
+    """The batched-inverse and adjoint restatements against numpy: inv(A) from the LU
+    factors, and G <- A^{-T} G, GA = -(A^{-T} G) X^T from the factors of a solve."""
+    rng = np.random.default_rng(200 + n)
+    A = rng.uniform(-1, 1, (n, n)) + 2 * np.eye(n)
+    S = np.ascontiguousarray(A.T)[None].copy()
+    X = rng.uniform(-1, 1, (1, 3, n))
+    ipiv, info = oracle.dgetrf_batched(S)
+    assert info[0] == 0
+    Inv = oracle.getri(S[0], ipiv[0])
+    ref = np.linalg.inv(A)
+    assert np.abs(Inv.T - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max()) * n
+    G = rng.standard_normal((1, 3, n))
+    Gc = G.copy()
+    GA = oracle.gesv_adjoint_batched(S, ipiv, X, Gc)
+    gb = np.linalg.solve(A.T, G[0].T)                       # (n, 3)
+    assert np.abs(Gc[0].T - gb).max() <= 1e-12 * max(1.0, np.abs(gb).max()) * n
+    ga = -gb @ X[0]                                         # (n, n) = -gb x^T
+    assert np.abs(GA[0].T - ga).max() <= 1e-12 * max(1.0, np.abs(ga).max()) * n
