@@ -107,3 +107,34 @@ def test_vbatched_tuning_table_roundtrip(lib):
         # autotune argument errors need no GPU
         assert getattr(lib, f"magma_{p}getrf_vbatched_autotune")(-1, None, None, None) == -1
         assert getattr(lib, f"magma_{p}getrf_vbatched_autotune")(64, None, None, None) == -4
+
+
+def test_header_is_c99_and_links(lib, tmp_path):
+    """A C caller: the header compiles as ISO C99 (-pedantic -Werror) and a program that
+    takes the addresses of the entry points links against libmagma_lu.so."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "magma_lu.h"\n'
+        "typedef magma_int_t (*gesv_fn)(magma_int_t, magma_int_t, double **, magma_int_t,\n"
+        "                               magma_int_t **, double **, magma_int_t, magma_int_t *,\n"
+        "                               magma_int_t, magma_queue_t);\n"
+        "static void (*volatile keep[3])(void);\n"
+        "int main(void) {\n"
+        "    gesv_fn f = magma_dgesv_batched;\n"
+        "    keep[0] = (void (*)(void))f;\n"
+        "    keep[1] = (void (*)(void))magma_dgetrf_batched;\n"
+        "    keep[2] = (void (*)(void))magma_dsposv_batched;\n"
+        "    return 0;\n"
+        "}\n")
+    from magma_gb300 import lib as L
+    inc = ROOT / "include"
+    libdir = L.LIB_PATH.parent
+    out = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{inc}",
+                          str(src), f"-L{libdir}", "-lmagma_lu", f"-Wl,-rpath,{libdir}", "-o",
+                          str(tmp_path / "caller")], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
