@@ -175,13 +175,12 @@ class Gesv32:
                 "hbm_frac_of_measured": nbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
 
     def cpu_sample(self, nthreads, target_s):
-        import oracle
         S_h, B_h = self.host_inputs()
 
         def run(k):
             s, x = S_h[:k].copy(), B_h[:k].copy()
             t0 = time.perf_counter()
-            oracle.dgesv_batched(s, x, nthreads=nthreads)
+            cpu_gesv(s, x, nthreads)
             return time.perf_counter() - t0
         k = min(self.batch, 1000)
         t = run(k)
@@ -404,7 +403,6 @@ class Dsgesv512:
                 **extra}
 
     def cpu_sample(self, nthreads, target_s):
-        import oracle
         if not hasattr(self, "_cpu_inputs"):
             A, B = self.gen("cpu")
             self._cpu_inputs = (A.transpose(1, 2).contiguous().numpy(),
@@ -414,13 +412,13 @@ class Dsgesv512:
         def run(k):
             s, x = S[:k].copy(), Bs[:k].copy()
             t0 = time.perf_counter()
-            oracle.dgesv_batched(s, x, nthreads=nthreads)
+            cpu_gesv(s, x, nthreads)
             return time.perf_counter() - t0
         k = max(nthreads, 1)
         t = run(k)
         k = int(min(self.batch, max(k, k * target_s / max(t, 1e-6))))
         ts = [run(k) for _ in range(3)]
-        return k, statistics.median(ts), f"{k} of the {self.batch} matrices (FP64 dgetrf+dgetrs)"
+        return k, statistics.median(ts), f"{k} of the {self.batch} matrices (FP64 dgesv)"
 
 
 class GesvVbatched:
@@ -564,14 +562,13 @@ class GesvVbatched:
                         "sort's share of the replay is in the launch-list summary"}
 
     def cpu_sample(self, nthreads, target_s):
-        import oracle
         ns, rs, As, Bs = self.host_inputs()
 
         def run(k):
             a = [x.copy() for x in As[:k]]
             b = [x.copy() for x in Bs[:k]]
             t0 = time.perf_counter()
-            oracle.dgesv_vbatched(ns[:k], rs[:k], a, b, nthreads=nthreads)
+            cpu_gesv_list(ns[:k], rs[:k], a, b, nthreads)
             return time.perf_counter() - t0
         k = 256
         t = run(k)
@@ -667,7 +664,6 @@ class Adjoint2048:
                 "fp64_tflops": flops / (ms_step * 1e-3) / 1e12}
 
     def cpu_sample(self, nthreads, target_s):
-        import oracle
         import torch
         g = torch.Generator(device="cpu").manual_seed(self.seed)
         b, n, r = self.batch, self.n, self.nrhs
@@ -682,8 +678,7 @@ class Adjoint2048:
         def run(k):
             S, X, G = S0[:k].copy(), X0[:k].copy(), G0[:k].copy()
             t0 = time.perf_counter()
-            ipiv, _ = oracle.dgesv_batched(S, X, nthreads=nthreads)
-            oracle.gesv_adjoint_batched(S, ipiv, X, G, nthreads=nthreads)
+            cpu_adjoint_list([n] * k, [r] * k, list(S), list(X), list(G), nthreads)
             return time.perf_counter() - t0
         k = 256
         t = run(k)
@@ -921,18 +916,15 @@ class Serve256:
                 "peak_source": "FP32 FMA-throughput probe run inside bench.py"}
 
     def cpu_sample(self, nthreads, target_s):
-        import oracle
         ns, As, Bs, Gs = self.host_inputs() if not hasattr(self, "_host") else self._host
         self._host = (ns, As, Bs, Gs)
 
         def run(k):
             a = [x.copy() for x in As[:k]]
             b = [x.copy() for x in Bs[:k]]
+            g = [x.copy() for x in Gs[:k]]
             t0 = time.perf_counter()
-            pivs, _ = oracle.dgesv_vbatched(ns[:k], [self.nrhs] * k, a, b, nthreads=nthreads)
-            for j in range(k):
-                oracle.gesv_adjoint_batched(a[j][None], pivs[j][None], b[j][None],
-                                            Gs[j][None].copy(), nthreads=1)
+            cpu_adjoint_list(ns[:k], [self.nrhs] * k, a, b, g, nthreads)
             return time.perf_counter() - t0
         k = 16
         t = run(k)
@@ -1121,22 +1113,72 @@ def measured_peaks(stream_handle):
 # CPU reference leg
 
 
-def cpu_baseline(wl, target_s=3.0):
+def cpu_kind():
+    """("lapack", description) when scipy's bundled LAPACK can be loaded: the reference's CPU
+    path itself (testing/testing_zgesv_batched.cpp:160-176: lapackf77_dgesv per matrix, OpenMP
+    schedule(dynamic), one BLAS thread); else ("port", ...) for the oracle's restatement."""
+    from oracle import lapack
+    if lapack.available():
+        return "lapack", (f"LAPACK dgesv per matrix ({lapack.library_name()}, scipy's bundled "
+                          f"OpenBLAS, one BLAS thread per call; the adjoint adds dgetrs('T') and "
+                          f"dger), OpenMP schedule(dynamic), as testing/testing_zgesv_batched.cpp:"
+                          f"160-176")
+    return "port", (f"oracle/lu_oracle.c dgetrf+dgetrs per matrix (restated reference CPU path; "
+                    f"scipy's LAPACK unavailable: {lapack.unavailable_reason()}), OpenMP "
+                    f"schedule(dynamic)")
+
+
+def cpu_threads():
+    from oracle import lapack
     import oracle
-    nthreads = oracle.max_threads()
+    return lapack.max_threads() if lapack.available() else oracle.max_threads()
+
+
+def cpu_gesv(S, X, nthreads):
+    """(batch, n, ld) / (batch, nrhs, ldb) FP64 column-major, in place, on the CPU path."""
+    from oracle import lapack
+    if lapack.available():
+        return lapack.dgesv_batched(S, X, nthreads=nthreads)
+    import oracle
+    return oracle.dgesv_batched(S, X, nthreads=nthreads)[1]
+
+
+def cpu_gesv_list(ns, rs, As, Bs, nthreads):
+    from oracle import lapack
+    if lapack.available():
+        return lapack.dgesv_list(As, Bs, nthreads=nthreads)
+    import oracle
+    return oracle.dgesv_vbatched(ns, rs, As, Bs, nthreads=nthreads)[1]
+
+
+def cpu_adjoint_list(ns, rs, As, Bs, Gs, nthreads):
+    """Forward solve, transposed solve and the outer product per matrix."""
+    from oracle import lapack
+    if lapack.available():
+        GAs = [np.empty_like(a) for a in As]
+        return lapack.dgesv_adjoint_list(As, Bs, Gs, GAs, nthreads=nthreads)
+    import oracle
+    pivs, info = oracle.dgesv_vbatched(ns, rs, As, Bs, nthreads=nthreads)
+    for j in range(len(As)):
+        oracle.gesv_adjoint_batched(As[j][None], pivs[j][None], Bs[j][None], Gs[j][None].copy(),
+                                    nthreads=1)
+    return info
+
+
+def cpu_baseline(wl, target_s=3.0):
+    nthreads = cpu_threads()
+    kind, how = cpu_kind()
     k, t, what = wl.cpu_sample(nthreads, target_s)
-    return {"value": k / t, "unit": "solves/s", "cores": nthreads, "kind": "port",
-            "sample": f"{what}: oracle/lu_oracle.c dgetrf+dgetrs per matrix (the reference's "
-                      f"CPU path, testing/testing_zgesv_batched.cpp:160-176, restated), OpenMP "
-                      f"schedule(dynamic) over {nthreads} threads, median of 3 passes"}
+    return {"value": k / t, "unit": "solves/s", "cores": nthreads, "kind": kind,
+            "sample": f"{what}: {how}, {nthreads} threads, median of 3 passes"}
 
 
 def run_reference(args, wl):
     world, rank, local, pg = dist_setup()
     if rank != 0:
         return 0
-    import oracle
-    nthreads = oracle.max_threads()
+    nthreads = cpu_threads()
+    kind, how = cpu_kind()
     k, t_probe, what = wl.cpu_sample(nthreads, target_s=2.0)
     vals = []
     for _ in range(args.warmup):
@@ -1152,10 +1194,9 @@ def run_reference(args, wl):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": wl.describe(), "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": kind,
                              "sample": f"each step: a bounded sample of the workload ({what}); "
-                                       f"oracle/lu_oracle.c dgetrf+dgetrs per matrix, OpenMP over "
-                                       f"{nthreads} host threads"},
+                                       f"{how}, {nthreads} host threads"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

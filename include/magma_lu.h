@@ -361,6 +361,15 @@ magma_int_t magma_sgetrf_batched_tc(magma_int_t precision, magma_int_t m, magma_
  * pipeline wait timed out); synchronises the queue. */
 magma_int_t magma_sgetrf_batched_tc_status(magma_int_t m, magma_int_t n, void *work,
                                            magma_int_t batchCount, magma_queue_t queue);
+/* No counterpart in the reference.  Self-test of the tensor-core kernels'
+ * bounded waits: one CTA takes tensor memory and waits, for at most
+ * limit_cycles SM clocks (1 .. 4e9), on an mbarrier that nothing arrives at
+ * (nothing is in flight), then records error 3 in *flag (one int of device
+ * memory), frees the tensor memory and returns.  Returns the recorded code (3
+ * when the wait ran out, as it must) or -1 / -2 for a bad limit / flag, and
+ * leaves the context usable.  Synchronises the queue. */
+magma_int_t magma_sgetrf_batched_tc_wait_selftest(long long limit_cycles, magma_int_t *flag,
+                                                  magma_queue_t queue);
 
 /* ------------------------------------------------------------------------ */
 /* Batched mixed-precision iterative refinement.  MAGMA refines one matrix
@@ -372,7 +381,12 @@ magma_int_t magma_sgetrf_batched_tc_status(magma_int_t m, magma_int_t n, void *w
  *   iter[k] = -2   A_k overflows in FP32;  -3  the FP32 LU hit a zero pivot;
  *   iter[k] = -itermax-1  no convergence.
  * For iter[k] < 0 the matrix is re-solved in FP64 (A_k overwritten by its
- * FP64 LU, info[k] from that factorisation), like zcgesv_gpu.cpp:352-362. */
+ * FP64 LU, info[k] from that factorisation), like zcgesv_gpu.cpp:352-362.
+ * Size limits (all of these routines and their adjoints): nrhs <= 16, and the
+ * order n such that one matrix's right-hand sides fit in shared memory -- on
+ * GB300 n <= 13999 for nrhs = 1, 12800 for 2, 6400 for 3..4, 3200 for 5..8,
+ * 1600 for 9..16; larger orders return MAGMA_ERR_NOT_SUPPORTED with a message
+ * naming the limit. */
 
 /* FP32 factorisation, FP64 residual, ITERMAX = 30, dsgesv stopping rule
  * ||r_c||_inf <= ||x_c||_inf * ||A||_inf * eps * sqrt(n) for every column c.
@@ -761,12 +775,21 @@ magma_int_t magma_svbatched_tuning_set(const magma_int_t *nb, const magma_int_t 
  * trailing update, 5 tensor-core trailing update, 6 triangular solves,
  * 7 refinement FP64 residual, 8 refinement correction solve, 9 refinement
  * conversion, 10 variable-size persistent factor+solve, 11 adjoint outer
- * product.  Returns -1 for a bad class, -2 for a bad capacity.
+ * product, 12 rank-128 update right of a 128-column block (FP32 LU: the
+ * block's interchanges, its U12 solve and its trailing update).  Returns -1 for a bad class, -2 for a bad capacity.
  *
  * magma_lu_timing_stop: waits for the recorded events, returns the number of
  * timed launches, the number dropped and their summed device time, and turns
  * timing off.  Use from one host thread. */
 long long magma_lu_launch_count(void);
+/* No counterpart in the reference.  Fault injection for tests: the next
+ * `count` device allocations the library makes for itself (queue workspaces,
+ * the autotuner's trial batches, the RBT butterflies) fail as if the device
+ * were out of memory, so the calls return MAGMA_ERR_DEVICE_ALLOC as the
+ * reference does when its workspace cannot be allocated
+ * (src/zgetrf_batched.cpp:137-142).  0 turns it off; returns the count that was
+ * still pending. */
+magma_int_t magma_lu_fail_allocations(magma_int_t count);
 magma_int_t magma_lu_timing_start(magma_int_t kernel_class, magma_int_t capacity);
 magma_int_t magma_lu_timing_stop(magma_int_t *launches, magma_int_t *dropped, double *total_ms);
 

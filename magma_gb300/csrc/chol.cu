@@ -181,8 +181,8 @@ magma_int_t chol_solve(int n, int nrhs, T **dA, int lda, T **dB, int ldb, int ba
                        magma_queue_t q)
 {
     const size_t smem = (size_t)CHOL_NR * n * sizeof(T);
-    static size_t dyn_max = 0;
-    if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(chol_solve_kernel<T>);
+    static size_t dyn_cache[MLU_MAX_DEVICES];
+    const size_t dyn_max = mlu_device_cached(dyn_cache, [] { return mlu_allow_dynamic_smem(chol_solve_kernel<T>); });
     if (smem > dyn_max) return MAGMA_ERR_NOT_SUPPORTED;
     const int threads = min(256, max(64, (n + 31) / 32 * 32));
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {

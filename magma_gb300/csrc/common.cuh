@@ -86,6 +86,20 @@ __device__ __forceinline__ unsigned warp_argmax_key(unsigned long long key, unsi
 template <typename T>
 __device__ __forceinline__ T shfl(T v, int src) { return __shfl_sync(FULL, v, src); }
 
+// cp.async of one element (4 or 8 bytes) to shared memory; `valid` false
+// writes zeros and reads nothing (src must still be a valid address).
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void *dst, const void *src, bool valid)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(src), "n"(BYTES),
+                 "r"(valid ? BYTES : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 }  // namespace mlu
 
 #define MLU_CHECK_LAUNCH()                                                              \
@@ -118,6 +132,36 @@ static inline size_t mlu_allow_dynamic_smem(K kernel)
     }
     return (size_t)dyn;
 }
+
+// Per-device cache of a value computed once per device by f(), such as the
+// dynamic shared memory a kernel may use after cudaFuncSetAttribute (which
+// applies to the current device only).  `cache` has MLU_MAX_DEVICES entries, all
+// zero at first; f() must return a non-zero value.  Two threads that race on
+// the first call both run f(), which is harmless for the attribute calls.
+constexpr int MLU_MAX_DEVICES = 64;
+template <typename F>
+static inline size_t mlu_device_cached(size_t *cache, F f)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MLU_MAX_DEVICES) {
+        cudaGetLastError();
+        return f();
+    }
+    size_t v = __atomic_load_n(&cache[dev], __ATOMIC_ACQUIRE);
+    if (v == 0) {
+        v = f();
+        __atomic_store_n(&cache[dev], v, __ATOMIC_RELEASE);
+    }
+    return v;
+}
+
+namespace mlu {
+// Every device allocation the library makes for itself (queue workspaces, the
+// autotuner's trial batches) goes through this wrapper, so that a test can make
+// the next allocations fail (magma_lu_fail_allocations) and check the
+// MAGMA_ERR_DEVICE_ALLOC path without exhausting a shared GPU.
+cudaError_t device_malloc(void **ptr, size_t bytes);
+}  // namespace mlu
 
 static inline magma_int_t mlu_max(magma_int_t a, magma_int_t b) { return a > b ? a : b; }
 static inline magma_int_t mlu_min(magma_int_t a, magma_int_t b) { return a < b ? a : b; }

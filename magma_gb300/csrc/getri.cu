@@ -68,8 +68,8 @@ static magma_int_t getri_run(const char *name, magma_int_t n, T **dA_array, magm
     }
     if (n == 0 || batchCount == 0) return 0;
     const size_t smem = (size_t)GETRI_NR * n * sizeof(T) + (size_t)n * sizeof(int);
-    static size_t dyn_max = 0;
-    if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(getri_kernel<T>);
+    static size_t dyn_cache[MLU_MAX_DEVICES];
+    const size_t dyn_max = mlu_device_cached(dyn_cache, [] { return mlu_allow_dynamic_smem(getri_kernel<T>); });
     if (smem > dyn_max) return MAGMA_ERR_NOT_SUPPORTED;
     const int threads = min(GETRI_THREADS, max(64, (n + 31) / 32 * 32));
     cudaStream_t s = queue->stream;

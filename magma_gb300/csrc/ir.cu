@@ -939,8 +939,8 @@ static void launch_residual(const IrShape &sh, double **dA, double **dB, double 
                             unsigned long long *stats, int par, int batch, cudaStream_t s)
 {
     const size_t smem = (size_t)sh.n * NR * sizeof(double);
-    static size_t dyn_max = 0;
-    if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(ir_residual_kernel<NR, TRANS>);
+    static size_t dyn_cache[MLU_MAX_DEVICES];
+    mlu_device_cached(dyn_cache, [] { return mlu_allow_dynamic_smem(ir_residual_kernel<NR, TRANS>); });
     MLU_LAUNCH(mlu::KC_IR_RESIDUAL, s,
                ir_residual_kernel<NR, TRANS><<<dim3((sh.n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS,
                                                smem, s>>>(sh, dA, dB, dX, R, stats, par));
@@ -984,26 +984,49 @@ static void correction_solve(const IrShape &sh, float **As_array, int ldas, cons
             sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, rsc, csc));
 }
 
+// Right-hand sides per CTA of the residual kernel for nrhs (residual()) and of
+// the correction solve (correction_solve()).
+static int residual_nr(int nrhs) { return nrhs <= 1 ? 1 : nrhs <= 2 ? 2 : nrhs <= 4 ? 4 : nrhs <= 8 ? 8 : 16; }
+static int solve_nr(int nrhs) { return nrhs <= 4 ? 4 : IR_SOLVE_NR; }
+constexpr size_t IR_RESIDUAL_SMEM_MAX = 200 * 1024;   // X rows of the residual, in shared memory
+
+static size_t solve_dyn_max();
+
+// The refinement keeps one matrix's right-hand sides in shared memory: n *
+// residual_nr(nrhs) doubles for the residual and n * solve_nr(nrhs) floats for
+// the correction solve.  False (with a message naming the largest order for
+// this nrhs) when n is too large for that.
+static bool ir_fits(const char *name, int n, int nrhs)
+{
+    const size_t rb = (size_t)residual_nr(nrhs) * sizeof(double), sb = (size_t)solve_nr(nrhs) * sizeof(float);
+    const size_t smax = solve_dyn_max();
+    if ((size_t)n * rb <= IR_RESIDUAL_SMEM_MAX && (size_t)n * sb <= smax) return true;
+    const size_t nmax = min(IR_RESIDUAL_SMEM_MAX / rb, smax / sb);
+    fprintf(stderr, "%s: order n=%d with nrhs=%d does not fit the refinement's shared-memory right-hand "
+                    "sides; the largest order for this nrhs is %zu\n", name, n, nrhs, nmax);
+    return false;
+}
+
 static size_t gm_dyn_max()
 {
-    static size_t v = 0;
-    if (!v)
-        v = min(mlu_allow_dynamic_smem(gm_correction_kernel<4>),
-                mlu_allow_dynamic_smem(gm_correction_kernel<8>));
-    return v;
+    static size_t cache[MLU_MAX_DEVICES];
+    return mlu_device_cached(cache, [] {
+        return min(mlu_allow_dynamic_smem(gm_correction_kernel<4>),
+                   mlu_allow_dynamic_smem(gm_correction_kernel<8>));
+    });
 }
 
 static size_t solve_dyn_max()
 {
-    static size_t v = 0;
-    if (!v)
-        v = min(min(min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false>),
-                        mlu_allow_dynamic_smem(ir_solve_kernel<4, false>)),
-                    min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, true>),
-                        mlu_allow_dynamic_smem(ir_solve_kernel<4, true>))),
-                min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false, true>),
-                    mlu_allow_dynamic_smem(ir_solve_kernel<4, false, true>)));
-    return v;
+    static size_t cache[MLU_MAX_DEVICES];
+    return mlu_device_cached(cache, [] {
+        return min(min(min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false>),
+                           mlu_allow_dynamic_smem(ir_solve_kernel<4, false>)),
+                       min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, true>),
+                           mlu_allow_dynamic_smem(ir_solve_kernel<4, true>))),
+                   min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false, true>),
+                       mlu_allow_dynamic_smem(ir_solve_kernel<4, false, true>)));
+    });
 }
 
 }  // namespace mlu
@@ -1034,9 +1057,7 @@ ir_run(int prec, const IrShape &sh, double **dA_array, magma_int_t **dipiv_array
     if (*lwork < L.total) return -15;
     if (n == 0 || nrhs == 0 || batchCount <= 0) return 0;
     // shared-memory limits of the correction solve and the residual kernels
-    if ((size_t)IR_SOLVE_NR * n * sizeof(float) > solve_dyn_max() ||
-        (size_t)n * IR_NRHS_MAX * sizeof(double) > 200 * 1024)
-        return MAGMA_ERR_NOT_SUPPORTED;
+    if (!ir_fits("magma_dxgesv_batched", n, nrhs)) return MAGMA_ERR_NOT_SUPPORTED;
     if (gm && (vb || nrhs > GM_NRHS_MAX || gm_smem_bytes<GM_NRHS_MAX>(n) > gm_dyn_max()))
         return MAGMA_ERR_NOT_SUPPORTED;
 
@@ -1219,9 +1240,7 @@ ir_run_adjoint(const IrShape &sh, double **dA_array, magma_int_t **dipiv_array, 
     const IrLayout L = ir_layout(n, nrhs, mlu_max(batchCount, 0), 900, vb);
     if (work == nullptr || lwork < L.total) return MAGMA_ERR_UNKNOWN;   // checked by the callers
     if (n == 0 || nrhs == 0 || batchCount <= 0) return 0;
-    if ((size_t)IR_SOLVE_NR * n * sizeof(float) > solve_dyn_max() ||
-        (size_t)n * IR_NRHS_MAX * sizeof(double) > 200 * 1024)
-        return MAGMA_ERR_NOT_SUPPORTED;
+    if (!ir_fits("magma_dxgesv_adjoint", n, nrhs)) return MAGMA_ERR_NOT_SUPPORTED;
     cudaStream_t s = queue->stream;
     char *w = (char *)work;
     unsigned long long *stats = (unsigned long long *)(w + L.stats);
@@ -1398,7 +1417,7 @@ magma_dsposv_batched(magma_uplo_t uplo, magma_int_t n, magma_int_t nrhs, double 
         }
         queue->work = nullptr;
         queue->work_bytes = 0;
-        if (cudaMalloc(&queue->work, lwork) != cudaSuccess) return MAGMA_ERR_DEVICE_ALLOC;
+        if (mlu::device_malloc(&queue->work, lwork) != cudaSuccess) return MAGMA_ERR_DEVICE_ALLOC;
         queue->work_bytes = lwork;
     }
     return magma_dsposv_batched_work(uplo, n, nrhs, dA_array, ldda, dB_array, lddb, dX_array,
@@ -1425,7 +1444,7 @@ magma_dsgesv_batched(magma_int_t n, magma_int_t nrhs, double **dA_array, magma_i
         }
         queue->work = nullptr;
         queue->work_bytes = 0;
-        if (cudaMalloc(&queue->work, lwork) != cudaSuccess) return MAGMA_ERR_DEVICE_ALLOC;
+        if (mlu::device_malloc(&queue->work, lwork) != cudaSuccess) return MAGMA_ERR_DEVICE_ALLOC;
         queue->work_bytes = lwork;
     }
     return magma_dsgesv_batched_work(n, nrhs, dA_array, ldda, dipiv_array, dB_array, lddb,

@@ -21,7 +21,10 @@
 // is only a stand-in for the device symbol), so the first call on each device
 // looks up the array's device address with cudaGetSymbolAddress, with that
 // device current, and keeps it; that first call on a device should come
-// before any stream capture.
+// before any stream capture.  The kept address belongs to the device's
+// primary context (the CUDA runtime's): a process that resets the device
+// (cudaDeviceReset) or runs the queue's stream in another context must not
+// call this entry afterwards, since the kept address would then be stale.
 //
 // Sharing.  Every call uses the same array and the array keeps whatever the
 // previous call left in it; the refinement clears everything that must start

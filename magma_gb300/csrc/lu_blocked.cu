@@ -37,26 +37,6 @@ namespace mlu {
 constexpr int PANEL_THREADS = PANEL_REGS_THREADS;
 constexpr int SWAP_THREADS = 128;
 
-// Per-matrix sizes for a variable-size batch (device arrays, or all null for a
-// uniform batch).  The step kernels take this matrix's m, n, ld from them, do
-// nothing when the matrix is already factored past column j0, and narrow the
-// panel to the matrix's last columns.
-struct StepSizes {
-    const int *m_arr, *n_arr, *ld_arr;
-    __device__ __forceinline__ bool get(int mat, int j0, int &m, int &n, int &ld, int &ib) const
-    {
-        if (m_arr) {
-            m = m_arr[mat];
-            n = n_arr[mat];
-            ld = ld_arr[mat];
-        }
-        const int mn = min(m, n);
-        if (j0 >= mn) return false;
-        ib = min(ib, mn - j0);
-        return true;
-    }
-};
-
 template <typename T, bool NOPIV = false>
 __global__ void __launch_bounds__(PANEL_THREADS)
 panel_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
@@ -123,13 +103,14 @@ constexpr int SWAP_COLS = 64;
 template <typename T>
 __global__ void __launch_bounds__(SWAP_THREADS)
 swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipiv_array,
-                 StepSizes vs, int with_left)
+                 StepSizes vs, int with_left, int bj)
 {
     __shared__ int s_row[2 * PANEL_NB], s_src[2 * PANEL_NB], s_cnt;
     __shared__ T s_tmp[2 * PANEL_NB * (SWAP_W + 1)];
     __shared__ T s_rhs[PANEL_NB * SWAP_COLS];
     const int mat = blockIdx.y;
     if (!vs.get(mat, j0, m, n, ldda, ib)) return;
+    n = block_col_end(bj, m, n);                     // right columns end with the block
     T *A = dA_array[mat];
     // column tile: left tiles cover [0, j0), right tiles cover [j0+ib, n)
     const int nleft = with_left ? (j0 + SWAP_COLS - 1) / SWAP_COLS : 0;
@@ -158,12 +139,13 @@ swap_trsm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int **ipi
 // A22 -= L21 * U12 on BM x BN tiles, TM x TN accumulators per thread.
 template <typename T, int BM, int BN, int TM, int TN>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
-gemm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int tiles_m, StepSizes vs)
+gemm_kernel(int m, int n, int j0, int ib, T **dA_array, int ldda, int tiles_m, StepSizes vs, int bj)
 {
     __shared__ __align__(16) T sL[PANEL_NB * BM];
     __shared__ __align__(16) T sU[BN * GEMM_LDU];
     const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
     if (!vs.get(blockIdx.y, j0, m, n, ldda, ib)) return;
+    n = block_col_end(bj, m, n);
     if (j0 + ib + tm * BM >= m || j0 + ib + tn * BN >= n) return;   // tile past this matrix
     gemm_tile<T, BM, BN, TM, TN>(dA_array[blockIdx.y], ldda, m, n, j0, ib, j0 + ib + tm * BM,
                                  j0 + ib + tn * BN, sL, sU);
@@ -222,22 +204,9 @@ __host__ __device__ constexpr size_t band_smem_bytes()
                             (size_t)PANEL_NB * (PANEL_NB + 1) + (size_t)BAND_WARPS * PANEL_NB * STRIP_M);
 }
 
-// cp.async of one element (4 or 8 bytes) to shared memory; `valid` false
-// writes zeros and reads nothing (src must still be a valid address).
-template <int BYTES>
-__device__ __forceinline__ void cp_async_elem(void *dst, const void *src, bool valid)
-{
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(src), "n"(BYTES),
-                 "r"(valid ? BYTES : 0)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
 __global__ void __launch_bounds__(BAND_THREADS, 2)
-band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv_array, StepSizes vs)
+band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv_array, StepSizes vs,
+            int bj)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *sU = reinterpret_cast<float *>(smem_raw);  // [PANEL_NB][BAND_U_LD]: U12, k-major
@@ -249,6 +218,7 @@ band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv
     __shared__ int s_row[PANEL_NB], s_src[PANEL_NB];
     const int mat = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (!vs.get(mat, j0, m, n, ldda, ib)) return;
+    n = block_col_end(bj, m, n);                     // columns right of the panel, up to the block's end
     const int c0 = j0 + ib + blockIdx.x * BAND_N;
     if (c0 >= n) return;                              // past this matrix's columns
     const int w = min(BAND_N, n - c0);
@@ -457,14 +427,23 @@ band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv
 // from the last to the first.  The columns then move through shared memory a
 // chunk at a time, coalesced both ways.  Rows per matrix: at most
 // LEFT_ROWS * LEFT_THREADS (2 or 4 rows per thread).
+//
+// With the two-level blocking (lu_outer.cu) the same gather runs in two parts:
+// LEFT_IN_BLOCK right after the panels of a 128-column block, for the block's
+// own later interchanges (k < the block's end), so that the block's columns
+// are in their final row order when the rank-128 update reads them; and
+// LEFT_AFTER_BLOCK after the last step, for the interchanges of the later
+// blocks (k >= the block's end).  LEFT_ALL does both at once (one-level
+// blocking).  `first`: the panel index of blockIdx.x = 0.
 constexpr int LEFT_THREADS = 256;
 constexpr int LEFT_DEFER_MAX_M = LEFT_THREADS * 4;
 constexpr size_t LEFT_BUF_BYTES = 24 * 1024;
+enum LeftMode { LEFT_ALL = 0, LEFT_IN_BLOCK = 1, LEFT_AFTER_BLOCK = 2 };
 
 template <typename T, int LEFT_ROWS>
 __global__ void __launch_bounds__(LEFT_THREADS)
 left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ipiv_array,
-                  StepSizes vs)
+                  StepSizes vs, int first, int mode)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sbuf = reinterpret_cast<T *>(smem_raw);        // [cols][seg]
@@ -473,7 +452,7 @@ left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ip
     const int mat = blockIdx.y, tid = threadIdx.x;
     if (tid == 0) {                                   // the panel's columns, as the steps chose them
         int j = 0;
-        for (int b = 0; b < (int)blockIdx.x; b++) j += blocked_panel_width<T>(gm, gn, j);
+        for (int b = 0; b < first + (int)blockIdx.x; b++) j += blocked_panel_width<T>(gm, gn, j);
         s_pj[0] = j;
         s_pj[1] = j + blocked_panel_width<T>(gm, gn, j);
     }
@@ -482,17 +461,21 @@ left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ip
     int ib = pj1 - pj0;
     if (!vs.get(mat, pj0, m, n, ldda, ib)) return;
     const int mn = min(m, n);
-    if (pj1 >= mn) return;                            // the matrix's last panel: nothing later
+    // interchanges ks .. ke-1 (rows ks..m-1 move)
+    const int bend = block_col_end(pj0 / OUTER_NB * OUTER_NB, m, n);
+    const int ks = mode == LEFT_AFTER_BLOCK ? bend : pj1;
+    const int ke = mode == LEFT_IN_BLOCK ? min(bend, mn) : mn;
+    if (ks >= ke) return;                             // nothing later
     T *A = dA_array[mat];
     const int *ipiv = ipiv_array[mat];
-    const int seg = m - pj1, nk = mn - pj1;
-    for (int k = tid; k < nk; k += LEFT_THREADS) s_piv[k] = ipiv[pj1 + k] - 1;
+    const int seg = m - ks, nk = ke - ks;
+    for (int k = tid; k < nk; k += LEFT_THREADS) s_piv[k] = ipiv[ks + k] - 1;
     __syncthreads();
     int tau[LEFT_ROWS];
 #pragma unroll
-    for (int u = 0; u < LEFT_ROWS; u++) tau[u] = pj1 + tid + u * LEFT_THREADS;
-    for (int k = mn - 1; k >= pj1; k--) {
-        const int p = s_piv[k - pj1];
+    for (int u = 0; u < LEFT_ROWS; u++) tau[u] = ks + tid + u * LEFT_THREADS;
+    for (int k = ke - 1; k >= ks; k--) {
+        const int p = s_piv[k - ks];
 #pragma unroll
         for (int u = 0; u < LEFT_ROWS; u++) tau[u] = tau[u] == k ? p : (tau[u] == p ? k : tau[u]);
     }
@@ -505,7 +488,7 @@ left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ip
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const int e = e0 + u * LEFT_THREADS;
-                if (e < total) v[u] = A[pj1 + e % seg + (size_t)(cb + e / seg) * ldda];
+                if (e < total) v[u] = A[ks + e % seg + (size_t)(cb + e / seg) * ldda];
             }
 #pragma unroll
             for (int u = 0; u < 8; u++) {
@@ -517,7 +500,7 @@ left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ip
         for (int c = 0; c < wc; c++) {
 #pragma unroll
             for (int u = 0; u < LEFT_ROWS; u++) {
-                const int i = pj1 + tid + u * LEFT_THREADS, src = tau[u] - pj1;
+                const int i = ks + tid + u * LEFT_THREADS, src = tau[u] - ks;
                 if (i < m && tau[u] != i && src >= 0 && src < seg)
                     A[i + (size_t)(cb + c) * ldda] = sbuf[c * seg + src];
             }
@@ -568,17 +551,17 @@ static void launch_panel(int rpt, int m, int n, int j0, int ib, T **dA, int ldda
 
 static int mlu_sm_count()
 {
-    static int count = 0;
-    if (!count) {
-        int dev = 0;
+    static size_t cache[MLU_MAX_DEVICES];
+    return (int)mlu_device_cached(cache, [] {
+        int dev = 0, count = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             count <= 0) {
             cudaGetLastError();
             count = 1;
         }
-    }
-    return count;
+        return (size_t)count;
+    });
 }
 
 // One step of the blocked factorisation for every matrix: panel at column j0
@@ -588,18 +571,20 @@ static int mlu_sm_count()
 // gemm_kernel (more, smaller CTAs) do.  `defer_left`: the interchanges left of
 // the panel are left to left_swaps_kernel after the last step.
 // `vsz`: per-matrix sizes of a variable-size batch (m, n = their maxima).
+// `bj` >= 0: the step is a panel of the block that starts at column bj, and
+// updates only the block's columns (block_col_end).
 template <typename T>
 magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, int *info, int batch,
                                   magma_queue_t q, int j0, int ib, bool update,
                                   StepSizes vsz = {nullptr, nullptr, nullptr},
-                                  bool defer_left = false)
+                                  bool defer_left = false, int bj = -1)
 {
     cudaStream_t s = q->stream;
     constexpr int BM = 64, BN = 64, TM = 4, TN = 4;
-    static size_t panel_dyn_max = 0;
-    if (!panel_dyn_max) {
-        panel_dyn_max = min(mlu_allow_dynamic_smem(panel_kernel<T, false>),
-                            mlu_allow_dynamic_smem(panel_kernel<T, true>));
+    static size_t panel_cache[MLU_MAX_DEVICES];
+    const size_t panel_dyn_max = mlu_device_cached(panel_cache, [] {
+        const size_t v = min(mlu_allow_dynamic_smem(panel_kernel<T, false>),
+                             mlu_allow_dynamic_smem(panel_kernel<T, true>));
         mlu_allow_dynamic_smem(panel_regs_kernel<T, 1, false>);
         mlu_allow_dynamic_smem(panel_regs_kernel<T, 2, false>);
         mlu_allow_dynamic_smem(panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2), false>);
@@ -607,7 +592,8 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
         mlu_allow_dynamic_smem(panel_regs_kernel<T, 2, true>);
         mlu_allow_dynamic_smem(panel_regs_kernel<T, (sizeof(T) == 4 ? 4 : 2), true>);
         if (band_used<T>()) mlu_allow_dynamic_smem(band_kernel);
-    }
+        return v;
+    });
     const int pm = m - j0;
     const int rpt = panel_rows_per_thread<T>(pm);
     const size_t smem = rpt == 1   ? panel_regs_smem_bytes<T, 1>()
@@ -634,7 +620,7 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
             launch_panel<T, true>(rpt, m, n, j0, ib, dAb, ldda, nullptr, infb, vs, nb, smem, s);
         else
             launch_panel<T, false>(rpt, m, n, j0, ib, dAb, ldda, ipb, infb, vs, nb, smem, s);
-        const int rm = m - j0 - ib, rn = n - j0 - ib;
+        const int rm = m - j0 - ib, rn = block_col_end(bj, m, n) - j0 - ib;
         const int bands = rn > 0 ? (rn + BAND_N - 1) / BAND_N : 0;
         const bool fused = band_used<T>() && update && bands > 0 &&
                            (long long)bands * nb >= 2LL * mlu_sm_count();
@@ -642,22 +628,22 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
         const int ncr = fused ? 0 : (rn + SWAP_COLS - 1) / SWAP_COLS;
         if (ncl + ncr > 0)
             MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, swap_trsm_kernel<T><<<dim3(ncl + ncr, nb), SWAP_THREADS, 0, s>>>(
-                m, n, j0, ib, dAb, ldda, ipb, vs, defer_left ? 0 : 1));
+                m, n, j0, ib, dAb, ldda, ipb, vs, defer_left ? 0 : 1, bj));
         if (fused) {
             MLU_LAUNCH(mlu::KC_GEMM, s, band_kernel<<<dim3(bands, nb), BAND_THREADS, band_smem_bytes(), s>>>(
-                m, n, j0, ib, reinterpret_cast<float **>(dAb), ldda, ipb, vs));
+                m, n, j0, ib, reinterpret_cast<float **>(dAb), ldda, ipb, vs, bj));
         } else if (update && rm > 0 && rn > 0) {
             if (rm <= 32 || rn <= 32) {
                 // a thin trailing block: 32 x 32 tiles, so that no FMA of a
                 // 64 x 64 tile runs on padding (each costs full FP64 issue slots)
                 const int tiles_m = (rm + 31) / 32, tiles_n = (rn + 31) / 32;
                 MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, 32, 32, 2, 2><<<dim3(tiles_m * tiles_n, nb), 256, 0, s>>>(
-                    m, n, j0, ib, dAb, ldda, tiles_m, vs));
+                    m, n, j0, ib, dAb, ldda, tiles_m, vs, bj));
             } else {
                 const int tiles_m = (rm + BM - 1) / BM, tiles_n = (rn + BN - 1) / BN;
                 MLU_LAUNCH(mlu::KC_GEMM, s, gemm_kernel<T, BM, BN, TM, TN><<<dim3(tiles_m * tiles_n, nb),
                                                                                 (BM / TM) * (BN / TN), 0, s>>>(
-                    m, n, j0, ib, dAb, ldda, tiles_m, vs));
+                    m, n, j0, ib, dAb, ldda, tiles_m, vs, bj));
             }
         }
     }
@@ -676,8 +662,11 @@ magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int 
 // `panels` panels the steps over max sizes (gm, gn) made.
 template <typename T>
 static magma_int_t launch_left_swaps(int m, int n, int gm, int gn, T **dA, int ldda, int **ipiv,
-                                     int batch, int panels, StepSizes vsz, cudaStream_t s)
+                                     int batch, int panels, StepSizes vsz, cudaStream_t s,
+                                     int first = 0, int mode = LEFT_ALL)
 {
+    // panels first .. first+panels-2 (the last panel has no later interchanges
+    // of its own block, and LEFT_AFTER_BLOCK is only called with all panels)
     if (panels < 2) return MAGMA_SUCCESS;
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
@@ -690,13 +679,66 @@ static magma_int_t launch_left_swaps(int m, int n, int gm, int gn, T **dA, int l
         if (gm <= 2 * LEFT_THREADS)
             MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, left_swaps_kernel<T, 2><<<dim3(panels - 1, nb), LEFT_THREADS,
                                                                        left_swaps_smem_bytes<T>(), s>>>(
-                m, n, gm, gn, dA + b0, ldda, ipiv + b0, vs));
+                m, n, gm, gn, dA + b0, ldda, ipiv + b0, vs, first, mode));
         else
             MLU_LAUNCH(mlu::KC_SWAP_TRSM, s, left_swaps_kernel<T, 4><<<dim3(panels - 1, nb), LEFT_THREADS,
                                                                        left_swaps_smem_bytes<T>(), s>>>(
-                m, n, gm, gn, dA + b0, ldda, ipiv + b0, vs));
+                m, n, gm, gn, dA + b0, ldda, ipiv + b0, vs, first, mode));
     }
     MLU_CHECK_LAUNCH();
+    return MAGMA_SUCCESS;
+}
+
+magma_int_t outer_update(int m, int n, int J, float **dA, int ldda, int **ipiv, StepSizes vs,
+                         int batch, magma_queue_t q);
+
+// The two-level blocking (lu_outer.cu) serves FP32 matrices of at most
+// LEFT_DEFER_MAX_M rows (register panels of width 32, interchanges left of the
+// panels deferred) with columns right of a first block.
+template <typename T>
+static bool outer_blocked(int m, int n)
+{
+    return sizeof(T) == 4 && m <= LEFT_DEFER_MAX_M && n > OUTER_NB && min(m, n) > PANEL_NB;
+}
+
+// Steps of the two-level blocked factorisation: per 128-column block, its
+// 32-column panels with updates confined to the block, then one rank-128
+// update of everything right of it; the interchanges left of each panel after
+// the last step, as in the one-level form.
+template <typename T>
+static magma_int_t blocked_getrf_outer(int m, int n, T **dA, int ldda, int **ipiv, int *info,
+                                       int batch, magma_queue_t q, StepSizes vs)
+{
+    const int mn = min(m, n);
+    int panels = 0;
+    for (int J = 0; J < mn; J += OUTER_NB) {
+        const int E = block_col_end(J, m, n);
+        const int first = panels;
+        for (int j0 = J; j0 < E; panels++) {
+            const int ib = blocked_panel_width<T>(m, n, j0);
+            const magma_int_t rc = blocked_getrf_steps_l<T>(m, n, dA, ldda, ipiv, info, batch, q, j0,
+                                                            ib, true, vs, true, J);
+            if (rc != 0) return rc;
+            j0 += ib;
+        }
+        // the block's own later interchanges on its earlier panels: L11 and L21
+        // in their final row order for the rank-128 update
+        if (ipiv != nullptr) {
+            const magma_int_t rc = launch_left_swaps<T>(m, n, m, n, dA, ldda, ipiv, batch, panels - first, vs,
+                                                        q->stream, first, LEFT_IN_BLOCK);
+            if (rc != 0) return rc;
+        }
+        if constexpr (sizeof(T) == 4) {
+            if (E < n || vs.m_arr) {
+                const magma_int_t rc = outer_update(m, n, J, dA, ldda, ipiv, vs, batch, q);
+                if (rc != 0) return rc;
+            }
+        }
+    }
+    // the later blocks' interchanges on every block's columns
+    if (ipiv != nullptr && mn > OUTER_NB)
+        return launch_left_swaps<T>(m, n, m, n, dA, ldda, ipiv, batch, panels, vs, q->stream, 0,
+                                    LEFT_AFTER_BLOCK);
     return MAGMA_SUCCESS;
 }
 
@@ -705,6 +747,8 @@ magma_int_t blocked_getrf(int m, int n, T **dA, int ldda, int **ipiv, int *info,
                           magma_queue_t q)
 {
     if (batch <= 0 || m == 0 || n == 0) return MAGMA_SUCCESS;
+    if (outer_blocked<T>(m, n))
+        return blocked_getrf_outer<T>(m, n, dA, ldda, ipiv, info, batch, q, {nullptr, nullptr, nullptr});
     const int mn = min(m, n);
     const bool defer = ipiv != nullptr && m <= LEFT_DEFER_MAX_M;
     int panels = 0;
@@ -739,6 +783,8 @@ magma_int_t blocked_getrf_vbatched(const int *m, const int *n, const int *ld, in
     if (batch <= 0 || max_m <= 0 || max_n <= 0) return MAGMA_SUCCESS;
     const int mn = min(max_m, max_n);
     const StepSizes vs = {m, n, ld};
+    if (outer_blocked<T>(max_m, max_n))
+        return blocked_getrf_outer<T>(max_m, max_n, dA, 0, ipiv, info, batch, q, vs);
     const bool defer = ipiv != nullptr && max_m <= LEFT_DEFER_MAX_M;
     int panels = 0;
     for (int j0 = 0; j0 < mn; panels++) {
@@ -802,14 +848,14 @@ magma_int_t blocked_getrs(bool trans, int n, int nrhs, T **dA, int ldda, int **i
     if (batch <= 0 || n == 0 || nrhs == 0) return MAGMA_SUCCESS;
     const int nr = nrhs <= 4 ? 4 : SOLVE_NR;
     const size_t smem = (size_t)nr * n * sizeof(T);
-    static size_t dyn_max[2][2] = {{0, 0}, {0, 0}};
-    size_t &dm = dyn_max[trans][nr == 4];
-    if (!dm) {
-        if (trans) dm = nr == 4 ? mlu_allow_dynamic_smem(getrs_kernel<T, true, 4>)
-                                : mlu_allow_dynamic_smem(getrs_kernel<T, true, SOLVE_NR>);
-        else dm = nr == 4 ? mlu_allow_dynamic_smem(getrs_kernel<T, false, 4>)
-                          : mlu_allow_dynamic_smem(getrs_kernel<T, false, SOLVE_NR>);
-    }
+    static size_t dyn_cache[2][2][MLU_MAX_DEVICES];
+    size_t *cache = dyn_cache[trans][nr == 4];
+    const size_t dm = mlu_device_cached(cache, [&] {
+        if (trans) return nr == 4 ? mlu_allow_dynamic_smem(getrs_kernel<T, true, 4>)
+                                  : mlu_allow_dynamic_smem(getrs_kernel<T, true, SOLVE_NR>);
+        return nr == 4 ? mlu_allow_dynamic_smem(getrs_kernel<T, false, 4>)
+                       : mlu_allow_dynamic_smem(getrs_kernel<T, false, SOLVE_NR>);
+    });
     if (smem > dm) return MAGMA_ERR_NOT_SUPPORTED;
     // one thread per row up to 256 (at least two warps: warp 0 solves the
     // diagonal blocks while the others wait)

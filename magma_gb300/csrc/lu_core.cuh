@@ -20,6 +20,39 @@ constexpr size_t PANEL_SMEM_MAX = 200 * 1024;   // shared memory for one panel
 constexpr int SWAP_W = 32;            // columns per gather/scatter chunk
 constexpr int GEMM_LDU = PANEL_NB + 4; // row stride of the transposed U12 tile in gemm_tile
 
+// Per-matrix sizes for a variable-size batch (device arrays, or all null for a
+// uniform batch).  The step kernels take this matrix's m, n, ld from them, do
+// nothing when the matrix is already factored past column j0, and narrow the
+// panel to the matrix's last columns.
+struct StepSizes {
+    const int *m_arr, *n_arr, *ld_arr;
+    __device__ __forceinline__ bool get(int mat, int j0, int &m, int &n, int &ld, int &ib) const
+    {
+        if (m_arr) {
+            m = m_arr[mat];
+            n = n_arr[mat];
+            ld = ld_arr[mat];
+        }
+        const int mn = min(m, n);
+        if (j0 >= mn) return false;
+        ib = min(ib, mn - j0);
+        return true;
+    }
+};
+
+// Two-level blocking of the FP32 factorisation: columns are factored in
+// blocks of OUTER_NB (four 32-column panels); inside a block the steps update
+// only the block's own columns, and the columns right of the block receive one
+// rank-OUTER_NB update per block (lu_outer.cu).  For a matrix with mn =
+// min(m, n), the block that starts at column bj ends at column
+// bj + min(OUTER_NB, mn - bj); bj < 0 means no outer blocking (the steps
+// update every column right of the panel).
+constexpr int OUTER_NB = 128;
+__host__ __device__ __forceinline__ int block_col_end(int bj, int m, int n)
+{
+    return bj < 0 ? n : min(n, bj + min(OUTER_NB, min(m, n) - bj));
+}
+
 // ---------------------------------------------------------------------------
 // NOPIV (both panels): the pivot of column k is the diagonal entry, as in
 // MAGMA's getrf_nopiv; a zero diagonal sets info and leaves the column

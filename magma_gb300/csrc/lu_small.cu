@@ -392,8 +392,9 @@ static void launch_small_gesv(int n, int nrhs, T **dA, int ldda, int **ipiv, T *
     if (N == 32) {   // 16 < n <= 32: the packed shared-memory kernel
         constexpr int NB = NRHS > 0 ? NRHS : 1;
         const size_t smem = (size_t)GESV_WARPS * packed_warp_elems<T>(NB) * sizeof(T);
-        static size_t dyn = 0;
-        if (!dyn) dyn = mlu_allow_dynamic_smem(small_gesv_packed_kernel<T, NRHS>);
+        static size_t dyn_cache[MLU_MAX_DEVICES];
+        const size_t dyn = mlu_device_cached(
+            dyn_cache, [] { return mlu_allow_dynamic_smem(small_gesv_packed_kernel<T, NRHS>); });
         if (smem <= dyn) {
             MLU_LAUNCH(mlu::KC_SMALL_GESV, s, small_gesv_packed_kernel<T, NRHS><<<mlu_ceildiv(batch, GESV_WARPS), GESV_WARPS * 32, smem, s>>>(
                 n, nrhs, dA, ldda, ipiv, dB, lddb, info, batch));

@@ -54,13 +54,13 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
                  "r"(bytes) : "memory");
 }
 
-// Wait for phase `parity` of the mbarrier, at most TC_WAIT_CYCLES SM clocks;
-// false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// Wait for phase `parity` of the mbarrier, at most `limit` SM clocks (by
+// default TC_WAIT_CYCLES); false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit = TC_WAIT_CYCLES)
 {
     const uint32_t addr = smem_u32(bar);
     const long long t0 = clock64();
-    while (clock64() - t0 < TC_WAIT_CYCLES) {
+    while (clock64() - t0 < limit) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -245,6 +245,38 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant_
 }
 
 // ---------------------------------------------------------------------------
+// Self-test of the bounded waits: one CTA takes tensor memory as the update
+// kernel does, then waits on an mbarrier that nothing arrives at (no copy and
+// no MMA is ever issued, so nothing is in flight when the wait gives up).  The
+// wait runs out after `limit` clocks, the CTA records error code 3, frees its
+// tensor memory and returns -- the path every real wait takes on a timeout.
+__global__ void __launch_bounds__(128, 1)
+tc_wait_selftest_kernel(long long limit, int *err)
+{
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_u32(&tmem_base)), "r"(32));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+    if (tid == 0 && !mbar_wait(&bar, 0, limit)) atomicExch(err, 3);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32));
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -329,8 +361,8 @@ static magma_int_t tc_getrf(int m, int n, float **dA, int ldda, int **ipiv, int 
     CUtensorMap mapL, mapU;
     if (!make_map(&mapL, Lb, L.pad, batch, BF16) || !make_map(&mapU, Ub, L.pad, batch, BF16))
         return MAGMA_ERR_NOT_SUPPORTED;
-    static size_t dyn = 0;
-    if (!dyn) dyn = mlu_allow_dynamic_smem(tc_update_kernel<BF16>);
+    static size_t dyn_cache[MLU_MAX_DEVICES];
+    const size_t dyn = mlu_device_cached(dyn_cache, [] { return mlu_allow_dynamic_smem(tc_update_kernel<BF16>); });
     // 2 x 8 KB of operands + alignment, requested as 56 KB so that at most four
     // CTAs share an SM: four 128-column accumulators fill its 512 TMEM columns
     const size_t smem = 56 * 1024;
@@ -396,6 +428,25 @@ extern "C" magma_int_t magma_sgetrf_batched_tc(magma_int_t precision, magma_int_
                          : tc_getrf<__half, false>(m, n, dA_array, ldda, ipiv_array, info_array,
                                                    batchCount, work, queue);
     return rc;
+}
+
+// Runs tc_wait_selftest_kernel with a wait limit of `limit_cycles` SM clocks
+// (1 .. 4e9) and returns the error code it recorded (3 when the wait ran out,
+// as it must), or a negative MAGMA error.  `flag`: one int of device memory.
+// Synchronises the queue.
+extern "C" magma_int_t magma_sgetrf_batched_tc_wait_selftest(long long limit_cycles, magma_int_t *flag,
+                                                             magma_queue_t queue)
+{
+    if (limit_cycles < 1 || limit_cycles > 4000000000ll) return -1;
+    if (flag == nullptr) return -2;
+    cudaMemsetAsync(flag, 0, sizeof(int), queue->stream);
+    MLU_LAUNCH(mlu::KC_OTHER, queue->stream,
+               tc_wait_selftest_kernel<<<1, 128, 0, queue->stream>>>(limit_cycles, flag));
+    MLU_CHECK_LAUNCH();
+    int e = 0;
+    cudaMemcpyAsync(&e, flag, sizeof(int), cudaMemcpyDeviceToHost, queue->stream);
+    if (cudaStreamSynchronize(queue->stream) != cudaSuccess) return MAGMA_ERR_UNKNOWN;
+    return e;
 }
 
 // Error flag of the last magma_sgetrf_batched_tc on this workspace (0 = fine);

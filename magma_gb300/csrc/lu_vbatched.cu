@@ -294,8 +294,8 @@ magma_int_t vb_run(const int *m, const int *n, const int *nrhs, int max_m, int m
             rc = vb_getrs_run<T>(false, n, nrhs, max_n, max_nrhs, dA, ldda, ipiv, dB, lddb, batch, q);
         return rc;
     }
-    static size_t dyn_max = 0;
-    if (!dyn_max) dyn_max = mlu_allow_dynamic_smem(vb_lu_kernel<T>);
+    static size_t dyn_cache[MLU_MAX_DEVICES];
+    const size_t dyn_max = mlu_device_cached(dyn_cache, [] { return mlu_allow_dynamic_smem(vb_lu_kernel<T>); });
     const size_t smem = min(vb_smem_bytes<T>(max_m, max_n, max_nrhs), dyn_max);
     // the panel of the largest matrix must fit with at least width 1
     if (max_m > VB_THREADS && panel_smem_bytes<T>(max_m, 1) > smem)
@@ -331,11 +331,10 @@ magma_int_t vb_getrs_run(bool trans, const int *n, const int *nrhs, int max_n, i
     if (batch <= 0 || max_n <= 0 || max_nrhs <= 0) return 0;
     const size_t smem = (size_t)VB_NR * max_n * sizeof(T);
     if (smem > VB_SMEM_CAP) return MAGMA_ERR_NOT_SUPPORTED;
-    static size_t dyn_max[2] = {0, 0};
-    if (!dyn_max[trans])
-        dyn_max[trans] = trans ? mlu_allow_dynamic_smem(vb_getrs_kernel<T, true>)
-                               : mlu_allow_dynamic_smem(vb_getrs_kernel<T, false>);
-    if (smem > dyn_max[trans]) return MAGMA_ERR_NOT_SUPPORTED;
+    static size_t dyn_cache[2][MLU_MAX_DEVICES];
+    const size_t dyn_max = trans ? mlu_device_cached(dyn_cache[1], [] { return mlu_allow_dynamic_smem(vb_getrs_kernel<T, true>); })
+                                 : mlu_device_cached(dyn_cache[0], [] { return mlu_allow_dynamic_smem(vb_getrs_kernel<T, false>); });
+    if (smem > dyn_max) return MAGMA_ERR_NOT_SUPPORTED;
     for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
         const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
         dim3 grid((max_nrhs + VB_NR - 1) / VB_NR, nb);
@@ -366,7 +365,7 @@ static magma_int_t vb_check(const int *m, const int *n, const int *nrhs, const i
         if (q->work) { cudaStreamSynchronize(q->stream); cudaFree(q->work); }
         q->work = nullptr;
         q->work_bytes = 0;
-        if (cudaMalloc(&q->work, 64) != cudaSuccess) return MAGMA_ERR_DEVICE_ALLOC;
+        if (mlu::device_malloc(&q->work, 64) != cudaSuccess) return MAGMA_ERR_DEVICE_ALLOC;
         q->work_bytes = 64;
     }
     stats = (int *)q->work;
@@ -385,7 +384,7 @@ static void *vb_queue_work(magma_queue_t q, int batch)
         if (q->work) { cudaStreamSynchronize(q->stream); cudaFree(q->work); }
         q->work = nullptr;
         q->work_bytes = 0;
-        if (cudaMalloc(&q->work, need) != cudaSuccess) return nullptr;
+        if (mlu::device_malloc(&q->work, need) != cudaSuccess) return nullptr;
         q->work_bytes = need;
     }
     return (char *)q->work + 256;
@@ -629,14 +628,14 @@ static magma_int_t vb_autotune(int max_n, magma_queue_t q, VbTune *out)
         int *P = nullptr, **dP = nullptr, *dn = nullptr, *dld = nullptr, *info = nullptr;
         void *work = nullptr;
         const size_t wb = vb_work_bytes(k);
-        if (cudaMalloc(&A, (size_t)k * n * n * sizeof(T)) != cudaSuccess ||
-            cudaMalloc(&P, (size_t)k * n * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&dA, k * sizeof(T *)) != cudaSuccess ||
-            cudaMalloc(&dP, k * sizeof(int *)) != cudaSuccess ||
-            cudaMalloc(&dn, k * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&dld, k * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&info, k * sizeof(int)) != cudaSuccess ||
-            cudaMalloc(&work, wb) != cudaSuccess) {
+        if (mlu::device_malloc((void **)&A, (size_t)k * n * n * sizeof(T)) != cudaSuccess ||
+            mlu::device_malloc((void **)&P, (size_t)k * n * sizeof(int)) != cudaSuccess ||
+            mlu::device_malloc((void **)&dA, k * sizeof(T *)) != cudaSuccess ||
+            mlu::device_malloc((void **)&dP, k * sizeof(int *)) != cudaSuccess ||
+            mlu::device_malloc((void **)&dn, k * sizeof(int)) != cudaSuccess ||
+            mlu::device_malloc((void **)&dld, k * sizeof(int)) != cudaSuccess ||
+            mlu::device_malloc((void **)&info, k * sizeof(int)) != cudaSuccess ||
+            mlu::device_malloc(&work, wb) != cudaSuccess) {
             cudaGetLastError();
             rc = MAGMA_ERR_DEVICE_ALLOC;
         }

@@ -251,7 +251,7 @@ extern "C" magma_int_t magma_dgerbt_batched(magma_bool_t gen, magma_int_t n, mag
     if (nrhs == 0 || n == 0) return 0;
     if (gen == MagmaTrue) init_butterfly(2 * n, U, V);
     double *d = nullptr;
-    if (cudaMalloc(&d, 4 * (size_t)n * sizeof(double)) != cudaSuccess) {
+    if (mlu::device_malloc((void **)&d, 4 * (size_t)n * sizeof(double)) != cudaSuccess) {
         cudaGetLastError();
         return *info = MAGMA_ERR_DEVICE_ALLOC;
     }
@@ -294,7 +294,7 @@ extern "C" magma_int_t magma_dgesv_rbt_batched(magma_int_t n, magma_int_t nrhs, 
                                                  lddb, dinfo_array, batchCount, queue);
     double *dv = nullptr;
     if (rc == 0 && n > 1) {
-        if (cudaMalloc(&dv, 2 * (size_t)n * sizeof(double)) != cudaSuccess) {
+        if (mlu::device_malloc((void **)&dv, 2 * (size_t)n * sizeof(double)) != cudaSuccess) {
             cudaGetLastError();
             rc = MAGMA_ERR_DEVICE_ALLOC;
         } else {

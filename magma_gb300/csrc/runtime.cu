@@ -8,7 +8,34 @@
 // struct around one cudaStream_t and carries no cuBLAS/cuSPARSE handles.
 #include "common.cuh"
 #include "trace.cuh"
+#include <atomic>
 #include <stdlib.h>
+
+namespace {
+std::atomic<int> g_fail_allocs{0};   // allocations still to fail (fault injection for tests)
+}
+
+cudaError_t mlu::device_malloc(void **ptr, size_t bytes)
+{
+    int left = g_fail_allocs.load();
+    while (left > 0 && !g_fail_allocs.compare_exchange_weak(left, left - 1)) {
+    }
+    if (left > 0) {
+        *ptr = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(ptr, bytes);
+}
+
+// Fault injection for tests: the next `count` device allocations the library
+// makes for itself fail as if the device were out of memory (the calls that
+// make them return MAGMA_ERR_DEVICE_ALLOC, as the reference does when its
+// pivot workspace cannot be allocated, src/zgetrf_batched.cpp:137-142).
+// count = 0 turns it off.  Returns the number that was still pending.
+extern "C" magma_int_t magma_lu_fail_allocations(magma_int_t count)
+{
+    return g_fail_allocs.exchange(count < 0 ? 0 : count);
+}
 
 extern "C" magma_int_t magma_init(void) {
     int count = 0;

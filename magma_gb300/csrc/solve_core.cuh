@@ -29,10 +29,24 @@ __device__ __forceinline__ void stage_diag_block(const T *A, int ldda, int t0, i
     __syncwarp();
 }
 
+// The same copy by cp.async (warp 0, one group per lane), so that the next
+// block's diagonal arrives while the current one is solved.
+template <typename T>
+__device__ __forceinline__ void stage_diag_block_async(const T *A, int ldda, int t0, int tb,
+                                                       T (*sD)[33])
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll 8
+    for (int c = 0; c < 32; c++)
+        if (c < tb && lane < tb) cp_async_elem<sizeof(T)>(&sD[lane][c], A + t0 + lane + (size_t)(t0 + c) * ldda, true);
+    cp_async_commit();
+}
+
 template <typename T, bool TRANS, int SOLVE_NR>
 __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, int nr)
 {
     __shared__ T sD[32][33];
+    __shared__ T sDD[2][32][33];      // double-buffered diagonal blocks (no transpose)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (!TRANS) {
         if (ipiv != nullptr && tid < nr) {
@@ -43,17 +57,34 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
             }
         }
         __syncthreads();
-        // forward: L y = b
-        for (int t0 = 0; t0 < n; t0 += 32) {
+        // forward: L y = b.  Per 32-row block: warp 0 solves the diagonal block
+        // (staged one block ahead by cp.async) while every thread already has
+        // the 32 coefficients of its first row below the block in flight; then
+        // all threads update the rows below.
+        if (warp == 0) stage_diag_block_async<T>(A, ldda, 0, min(32, n), sDD[0]);
+        for (int t0 = 0, blk = 0; t0 < n; t0 += 32, blk++) {
             const int tb = min(32, n - t0);
+            const int i0 = t0 + tb + tid;
+            T lv[32];
+            if (tb == 32 && i0 < n) {
+#pragma unroll
+                for (int t = 0; t < 32; t++) lv[t] = A[i0 + (size_t)(t0 + t) * ldda];
+            }
             if (warp == 0) {
+                if (t0 + 32 < n) {
+                    stage_diag_block_async<T>(A, ldda, t0 + 32, min(32, n - t0 - 32), sDD[(blk + 1) & 1]);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
+                __syncwarp();
+                T (*D)[33] = sDD[blk & 1];
                 T y[SOLVE_NR];
                 const bool v = lane < tb;
-                stage_diag_block<T>(A, ldda, t0, tb, sD);
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
                 for (int t = 0; t < tb; t++) {
-                    const T l = v ? sD[lane][t] : T(0);   // L(t0+lane, t0+t)
+                    const T l = v ? D[lane][t] : T(0);    // L(t0+lane, t0+t)
 #pragma unroll
                     for (int c = 0; c < SOLVE_NR; c++) {
                         const T yt = __shfl_sync(FULL, y[c], t);
@@ -64,15 +95,16 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 for (int c = 0; c < SOLVE_NR; c++) if (v) sB[c * n + t0 + lane] = y[c];
             }
             __syncthreads();
-            for (int i = t0 + tb + tid; i < n; i += blockDim.x) {
+            for (int i = i0; i < n; i += blockDim.x) {
                 T acc[SOLVE_NR];
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
                 if (tb == 32) {
-                    // the row's 32 coefficients in flight together, then the updates
-                    T lv[32];
+                    // the row's 32 coefficients (the first row's are already here)
+                    if (i != i0) {
 #pragma unroll
-                    for (int t = 0; t < 32; t++) lv[t] = A[i + (size_t)(t0 + t) * ldda];
+                        for (int t = 0; t < 32; t++) lv[t] = A[i + (size_t)(t0 + t) * ldda];
+                    }
 #pragma unroll
                     for (int t = 0; t < 32; t++)
 #pragma unroll
@@ -91,13 +123,27 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
             }
             __syncthreads();
         }
-        // backward: U x = y
-        for (int t1 = n; t1 > 0; t1 -= 32) {
+        // backward: U x = y, the same overlap (blocks from the bottom)
+        if (warp == 0) stage_diag_block_async<T>(A, ldda, max(0, n - 32), n - max(0, n - 32), sDD[0]);
+        for (int t1 = n, blk = 0; t1 > 0; t1 -= 32, blk++) {
             const int t0 = max(0, t1 - 32), tb = t1 - t0;
+            T uv0[32];
+            if (tb == 32 && tid < t0) {
+#pragma unroll
+                for (int t = 0; t < 32; t++) uv0[t] = A[tid + (size_t)(t0 + t) * ldda];
+            }
             if (warp == 0) {
+                if (t0 > 0) {
+                    const int p0 = max(0, t0 - 32);
+                    stage_diag_block_async<T>(A, ldda, p0, t0 - p0, sDD[(blk + 1) & 1]);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
+                __syncwarp();
+                T (*sD)[33] = sDD[blk & 1];
                 T y[SOLVE_NR];
                 const bool v = lane < tb;
-                stage_diag_block<T>(A, ldda, t0, tb, sD);
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
                 // lane t holds U(t0+t, t0+t) and its reciprocal, computed in parallel
@@ -123,14 +169,15 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
                 if (tb == 32) {
-                    T uv[32];
+                    if (i != tid) {
 #pragma unroll
-                    for (int t = 0; t < 32; t++) uv[t] = A[i + (size_t)(t0 + t) * ldda];
+                        for (int t = 0; t < 32; t++) uv0[t] = A[i + (size_t)(t0 + t) * ldda];
+                    }
 #pragma unroll
                     for (int t = 31; t >= 0; t--)
 #pragma unroll
                         for (int c = 0; c < SOLVE_NR; c++)
-                            acc[c] = Prec<T>::fma_(-uv[t], sB[c * n + t0 + t], acc[c]);
+                            acc[c] = Prec<T>::fma_(-uv0[t], sB[c * n + t0 + t], acc[c]);
                 } else {
                     for (int t = tb - 1; t >= 0; t--) {
                         const T u = A[i + (size_t)(t0 + t) * ldda];

@@ -50,7 +50,7 @@ static void **strided_scratch(magma_queue_t q, int batch)
         if (q->work) { cudaStreamSynchronize(q->stream); cudaFree(q->work); }
         q->work = nullptr;
         q->work_bytes = 0;
-        if (cudaMalloc(&q->work, need) != cudaSuccess) return nullptr;
+        if (mlu::device_malloc(&q->work, need) != cudaSuccess) return nullptr;
         q->work_bytes = need;
     }
     return (void **)q->work;

@@ -24,7 +24,8 @@ enum KernelClass {
     KC_IR_INIT = 9,       // FP64 -> low-precision conversion, norms
     KC_VB_LU = 10,        // persistent variable-size factor+solve
     KC_ADJ_GER = 11,      // adjoint outer product
-    KC_COUNT = 12
+    KC_OUTER = 12,        // rank-128 update right of a block of the FP32 LU (lu_outer.cu)
+    KC_COUNT = 13
 };
 
 void trace_before(int cls, cudaStream_t s);

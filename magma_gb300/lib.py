@@ -137,6 +137,8 @@ _PROTOS["magma_dsposv_batched_work"] = ([c_int, c_int, c_int, c_ptr, c_int, c_pt
 _PROTOS["magma_dsposv_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, c_int,
                                     c_ptr, c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
+_PROTOS["magma_lu_fail_allocations"] = ([c_int], c_int)
+_PROTOS["magma_sgetrf_batched_tc_wait_selftest"] = ([C.c_longlong, c_ptr, c_ptr], c_int)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
 _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTER(C.c_double)],
                                    c_int)
@@ -144,7 +146,7 @@ _PROTOS["magma_lu_timing_stop"] = ([C.POINTER(c_int), C.POINTER(c_int), C.POINTE
 # kernel classes of magma_lu_timing_start
 KERNEL_CLASSES = {"small_gesv": 1, "panel": 2, "swap_trsm": 3, "gemm": 4, "tc_update": 5,
                   "getrs": 6, "ir_residual": 7, "ir_solve": 8, "ir_init": 9, "vb_lu": 10,
-                  "adj_ger": 11}
+                  "adj_ger": 11, "outer": 12}
 
 
 def load(path: str | os.PathLike | None = None) -> C.CDLL:

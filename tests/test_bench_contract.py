@@ -1,6 +1,7 @@
 """The reference arm of bench.py runs on the host cores: its one JSON line keeps
 the keys the benchmark contract names (metric, value, unit, timing, config,
-cpu_baseline with kind "port", e2e with zero transfer bytes, impl)."""
+cpu_baseline with kind "lapack" -- the reference tester's LAPACK dgesv loop, or
+"port" where scipy's LAPACK is missing -- e2e with zero transfer bytes, impl)."""
 import json
 import subprocess
 import sys
@@ -22,7 +23,9 @@ def test_reference_arm_json_line():
         assert key in d, key
     assert d["impl"] == "reference"
     assert d["value"] > 0 and d["higher_is_better"] is True
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    from oracle import lapack
+    assert d["cpu_baseline"]["kind"] == ("lapack" if lapack.available() else "port")
+    assert d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0

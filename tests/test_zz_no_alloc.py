@@ -24,19 +24,30 @@ def _vp(t):
     return C.c_void_p(t.data_ptr())
 
 
-def _noalloc(S, B, cuda):
+def _buffers(S, B, cuda):
     b, n, ld = S.shape
-    nrhs, ldb = B.shape[1], B.shape[2]
     X = torch.empty_like(B)
     ipiv = torch.empty((b, n), dtype=torch.int32, device=cuda)
     info = torch.empty((b,), dtype=torch.int32, device=cuda)
     iters = torch.empty((b,), dtype=torch.int32, device=cuda)
-    dA, dP, dB, dX = ptr_array(S), ptr_array(ipiv), ptr_array(B), ptr_array(X)
-    rc = L.load().magma_dsgesv_batched_noalloc(n, nrhs, _vp(dA), ld, _vp(dP), _vp(dB), ldb,
-                                               _vp(dX), X.shape[2], _vp(info), _vp(iters), b,
-                                               Queue.current(cuda).handle)
+    return {"S": S, "B": B, "X": X, "ipiv": ipiv, "info": info, "iters": iters,
+            "dA": ptr_array(S), "dP": ptr_array(ipiv), "dB": ptr_array(B), "dX": ptr_array(X)}
+
+
+def _call(buf, queue):
+    b, n, ld = buf["S"].shape
+    nrhs, ldb = buf["B"].shape[1], buf["B"].shape[2]
+    rc = L.load().magma_dsgesv_batched_noalloc(n, nrhs, _vp(buf["dA"]), ld, _vp(buf["dP"]),
+                                               _vp(buf["dB"]), ldb, _vp(buf["dX"]), buf["X"].shape[2],
+                                               _vp(buf["info"]), _vp(buf["iters"]), b, queue.handle)
     torch.cuda.synchronize()
-    return rc, X, ipiv, info, iters
+    return rc
+
+
+def _noalloc(S, B, cuda):
+    buf = _buffers(S, B, cuda)
+    rc = _call(buf, Queue.current(cuda))
+    return rc, buf["X"], buf["ipiv"], buf["info"], buf["iters"]
 
 
 def _inputs(seed, batch, n, nrhs, cuda):
@@ -61,12 +72,31 @@ def test_noalloc_matches_work_entry_two_calls(cuda):
         assert torch.equal(S, S_ref) and torch.equal(B, B_ref)
 
 
+def test_noalloc_leaves_free_device_memory_unchanged(cuda):
+    """The defining property: a successful call allocates nothing, neither in the call
+    nor in the queue (a fresh queue, whose workspace stays empty)."""
+    S, B = _inputs(13, 32, 80, 2, cuda)
+    buf = _buffers(S.clone(), B, cuda)
+    q = Queue(cuda.index or 0, torch.cuda.current_stream(cuda).cuda_stream)
+    assert _call(buf, q) == 0             # first call on the device: symbol lookup, module loads
+    buf["S"].copy_(S)
+    free0 = torch.cuda.mem_get_info(cuda)[0]
+    assert _call(buf, q) == 0
+    free1 = torch.cuda.mem_get_info(cuda)[0]
+    assert free1 == free0
+    assert int(buf["iters"].min()) >= 0
+
+
 def test_noalloc_rejects_batches_beyond_the_scratch(cuda, capfd):
-    # 512 matrices of n = 512 need about 0.5 GiB of scratch, far above the fixed array
+    # 512 matrices of n = 512 need about 0.5 GiB of scratch, far above the fixed array;
+    # the size is refused on the host before any pointer is read, so every entry of the
+    # pointer arrays names the same small matrix
     need = mg.dsgesv_workspace_bytes(512, 4, 512)
     assert need > (32 << 20)
-    S = torch.zeros((512, 512, 512), dtype=torch.float64, device=cuda)
-    B = torch.zeros((512, 4, 512), dtype=torch.float64, device=cuda)
-    rc = _noalloc(S, B, cuda)[0]
+    A1 = torch.zeros((1, 512, 512), dtype=torch.float64, device=cuda)
+    B1 = torch.zeros((1, 4, 512), dtype=torch.float64, device=cuda)
+    buf = _buffers(A1.expand(512, 512, 512), B1.expand(512, 4, 512), cuda)   # stride 0: aliases
+    assert int(buf["dA"].min()) == int(buf["dA"].max()) == A1.data_ptr()
+    rc = _call(buf, Queue.current(cuda))
     assert rc == -103
     assert "static scratch" in capfd.readouterr().err
