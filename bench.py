@@ -266,6 +266,38 @@ class Dsgesv512:
 
     dominant_class = "ir_residual"
     dominant = "mlu::ir_residual_kernel<4> (FP64 residual R = B - A X)"
+    # kernel classes timed one at a time in extra calls after the timed region
+    breakdown_classes = ("ir_residual", "outer", "ir_solve", "gemm", "panel", "swap_trsm", "ir_init")
+
+    def outer_flops(self):
+        """Algorithmic flops of the rank-128 updates (U12 solve + A22 update) of one FP32
+        factorisation of order n, two-level blocked (128-column blocks): 2 FMA counts."""
+        n, fmas = self.n, 0
+        for J in range(0, n, 128):
+            K = min(128, n - J)
+            E = J + K
+            if E < n:
+                fmas += K * (K - 1) // 2 * (n - E) + (n - E) * (n - E) * K
+        return 2.0 * fmas
+
+    def restore(self, c, i):
+        """A private copy back to the input (a matrix that fell back to FP64 has its A
+        overwritten by FP64 factors)."""
+        c["Ss"][i].copy_(c["S"])
+
+    def secondary_roofline(self, times, peaks):
+        """The rank-128 update kernel (FP32 SIMT FMA): its algorithmic flops per step over
+        its measured time per step, against the FP32 FMA rate probed in the same run."""
+        if "outer" not in times or times["outer"] <= 0:
+            return None
+        flops = self.outer_flops() * self.batch
+        ach = flops / (times["outer"] * 1e-3) / 1e12
+        return {"kernel": "mlu::outer_update_kernel (FP32 interchanges + U12 solve + rank-128 "
+                          "A22 update)", "bound": "fp32", "achieved": ach,
+                "peak": peaks["fp32_tflops"], "unit": "TFLOP/s", "frac": ach / peaks["fp32_tflops"],
+                "algorithmic_flops_per_step": flops, "ms_per_step": times["outer"],
+                "peak_source": "FP32 FMA-throughput probe run inside bench.py "
+                               "(magma_gb300/probe/peaks.cu)"}
 
     # End to end: the batch goes through the C ABI as two calls, the first on a quarter
     # of the matrices; all host-to-device copies are queued at once on a copy stream,
@@ -1289,6 +1321,24 @@ def run_ours(args, wl):
     value, ms = aggregate_rate(pg, n_ok * args.steps, start.elapsed_time(end), dev)
     ms_per_step = ms / args.steps
 
+    # device time per kernel class, one class per extra call (outside the timed region)
+    breakdown = {}
+    if getattr(wl, "breakdown_classes", None) and not getattr(args, "no_breakdown", False):
+        i_extra = nsteps - 1
+        for cls in wl.breakdown_classes:
+            wl.restore(c, i_extra)
+            torch.cuda.synchronize(dev)
+            kt = KernelTimer(lib, cls)
+            kt.start()
+            wl.step(c, i_extra)
+            try:
+                kk = kt.stop(1)
+            except RuntimeError:          # no launch of this class in the call
+                kk = None
+            breakdown[cls] = kk["ms"] if kk else 0.0
+        wl.restore(c, i_extra)
+        torch.cuda.synchronize(dev)
+
     # end to end through the C ABI with pinned host buffers
     h2d, d2h = wl.e2e_setup(c)
     for _ in range(max(args.warmup, 1)):
@@ -1333,6 +1383,11 @@ def run_ours(args, wl):
                      **extra},
         "peaks_measured": peaks,
     }
+    if breakdown:
+        line["kernel_class_ms_per_step"] = breakdown
+        sec = wl.secondary_roofline(breakdown, peaks)
+        if sec is not None:
+            line["roofline_secondary"] = sec
     if fp64 is not None:
         line["fp64_path"] = fp64
         line["speedup_vs_fp64_path"] = value / fp64["value"] if fp64["value"] > 0 else None

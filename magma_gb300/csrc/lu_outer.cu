@@ -19,7 +19,7 @@
 //        by one thread per column, then a rank-32 update of the rows below);
 //     3. sweeps the rows below the block in 128-row tiles: the A22 tile lives
 //        in registers (8 x 8 elements per thread), L21 streams through shared
-//        memory in 16-column stages (cp.async, a ring of four, continuous
+//        memory in 32-column stages (cp.async, double-buffered and continuous
 //        across the tiles), and every element is updated acc = fma(-l, u, acc)
 //        for k ascending;
 //     4. writes U12 back last, so that a row below that receives an original
@@ -39,8 +39,8 @@ namespace mlu {
 constexpr int OB_TN = 128;                   // columns per CTA
 constexpr int OB_TM = 128;                   // rows of A22 per sweep tile
 constexpr int OB_KC = 32;                    // columns of L11 per diagonal block of the solve
-constexpr int OB_SK = 16;                    // columns of L21 per sweep stage
-constexpr int OB_RING = 4;                   // sweep stages in flight (ring)
+constexpr int OB_SK = 32;                    // columns of L21 per sweep stage
+constexpr int OB_RING = 2;                   // sweep stages in flight (ring)
 constexpr int OB_THREADS = 256;
 constexpr int OB_MAX_ROWS = 1024;            // rows per matrix (register panels, deferred interchanges)
 constexpr int OB_U_FLOATS = OUTER_NB * OB_TN;
@@ -48,7 +48,7 @@ constexpr int OB_STAGE_FLOATS = OB_KC * OB_TM;     // one L11 stage of the solve
 constexpr int OB_SSTAGE_FLOATS = OB_SK * OB_TM;    // one L21 stage of the sweep (four of them)
 constexpr size_t OB_SMEM = sizeof(float) * (OB_U_FLOATS + 2 * OB_STAGE_FLOATS);   // 96 KB
 static_assert(OB_TM == 128 && OB_TN == 128 && OB_THREADS == 256, "8 x 8 elements per thread");
-static_assert(OB_RING * OB_SSTAGE_FLOATS == 2 * OB_STAGE_FLOATS, "the ring reuses the solve's stages");
+static_assert(OB_RING * OB_SSTAGE_FLOATS <= 2 * OB_STAGE_FLOATS, "the ring reuses the solve's stages");
 static_assert(OUTER_NB % OB_SK == 0 && OB_SK % 8 == 0, "sweep stages");
 
 // Index of U12 element (k, c) in shared memory.  Groups of four columns (16
@@ -281,9 +281,9 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
     }
 
     // 4. A22 -= L21 U12, 128 rows at a time.  L21 streams through a ring of
-    //    OB_RING stages of 16 columns, continuous across the row tiles: stage g
-    //    holds columns J + 16 (g mod nsk) of tile g / nsk, issued three stages
-    //    ahead; one barrier per stage.
+    //    OB_RING stages of OB_SK columns, continuous across the row tiles: stage
+    //    g holds columns J + OB_SK (g mod nsk) of tile g / nsk and is issued
+    //    OB_RING - 1 stages ahead; one barrier per stage.
     const int below = m - E;
     const int ntiles = below > 0 ? (below + OB_TM - 1) / OB_TM : 0;
     const int nsk = (K + OB_SK - 1) / OB_SK;       // stages per tile
@@ -346,13 +346,13 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
                 }
             }
         }
-        cp_async_wait<OB_RING - 2>();             // stage g has landed (two younger in flight)
+        cp_async_wait<OB_RING - 2>();             // stage g has landed (younger ones may be in flight)
         __syncthreads();                          // ... for every thread; stage g-1 is free
         stage_l21(g + OB_RING - 1);
         const float *Lc = sL + (g % OB_RING) * OB_SSTAGE_FLOATS;
         const int kt = min(OB_SK, K - OB_SK * kc);
         if (kt == OB_SK) {
-#pragma unroll
+#pragma unroll 8
             for (int t = 0; t < OB_SK; t++) {
                 const int k = OB_SK * kc + t;
                 const float4 la = *reinterpret_cast<const float4 *>(Lc + t * OB_TM + tr * 4);

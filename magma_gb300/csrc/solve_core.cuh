@@ -83,12 +83,25 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 const bool v = lane < tb;
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
-                for (int t = 0; t < tb; t++) {
-                    const T l = v ? D[lane][t] : T(0);    // L(t0+lane, t0+t)
+                if (tb == 32) {
+                    // unrolled: the coefficient loads run ahead of the shuffle chain
 #pragma unroll
-                    for (int c = 0; c < SOLVE_NR; c++) {
-                        const T yt = __shfl_sync(FULL, y[c], t);
-                        if (v && lane > t) y[c] = Prec<T>::fma_(-l, yt, y[c]);
+                    for (int t = 0; t < 32; t++) {
+                        const T l = D[lane][t];            // L(t0+lane, t0+t)
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++) {
+                            const T yt = __shfl_sync(FULL, y[c], t);
+                            if (lane > t) y[c] = Prec<T>::fma_(-l, yt, y[c]);
+                        }
+                    }
+                } else {
+                    for (int t = 0; t < tb; t++) {
+                        const T l = v ? D[lane][t] : T(0);    // L(t0+lane, t0+t)
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++) {
+                            const T yt = __shfl_sync(FULL, y[c], t);
+                            if (v && lane > t) y[c] = Prec<T>::fma_(-l, yt, y[c]);
+                        }
                     }
                 }
 #pragma unroll
@@ -149,15 +162,31 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 // lane t holds U(t0+t, t0+t) and its reciprocal, computed in parallel
                 const T dl = v ? sD[lane][lane] : T(1);
                 const T rl = T(1) / dl;
-                for (int t = tb - 1; t >= 0; t--) {
-                    const T u = v ? sD[lane][t] : T(0);   // U(t0+lane, t0+t)
-                    const T d = __shfl_sync(FULL, dl, t);
-                    const T r = __shfl_sync(FULL, rl, t);
+                if (tb == 32) {
+                    // unrolled: coefficient loads and the diagonal shuffles run ahead
 #pragma unroll
-                    for (int c = 0; c < SOLVE_NR; c++) {
-                        const T x = rscale(__shfl_sync(FULL, y[c], t), d, r);
-                        if (lane == t) y[c] = x;
-                        else if (v && lane < t) y[c] = Prec<T>::fma_(-u, x, y[c]);
+                    for (int t = 31; t >= 0; t--) {
+                        const T u = sD[lane][t];           // U(t0+lane, t0+t)
+                        const T d = __shfl_sync(FULL, dl, t);
+                        const T r = __shfl_sync(FULL, rl, t);
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++) {
+                            const T x = rscale(__shfl_sync(FULL, y[c], t), d, r);
+                            if (lane == t) y[c] = x;
+                            else if (lane < t) y[c] = Prec<T>::fma_(-u, x, y[c]);
+                        }
+                    }
+                } else {
+                    for (int t = tb - 1; t >= 0; t--) {
+                        const T u = v ? sD[lane][t] : T(0);   // U(t0+lane, t0+t)
+                        const T d = __shfl_sync(FULL, dl, t);
+                        const T r = __shfl_sync(FULL, rl, t);
+#pragma unroll
+                        for (int c = 0; c < SOLVE_NR; c++) {
+                            const T x = rscale(__shfl_sync(FULL, y[c], t), d, r);
+                            if (lane == t) y[c] = x;
+                            else if (v && lane < t) y[c] = Prec<T>::fma_(-u, x, y[c]);
+                        }
                     }
                 }
 #pragma unroll

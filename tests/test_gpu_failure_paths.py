@@ -63,8 +63,10 @@ def test_tensor_core_factorisation_reports_no_timeout(cuda):
     work = torch.empty((lw.value,), dtype=torch.uint8, device=cuda)
     ipiv = torch.empty((b, n), dtype=torch.int32, device=cuda)
     info = torch.empty((b,), dtype=torch.int32, device=cuda)
-    rc = lib.magma_sgetrf_batched_tc(930, n, n, _vp(ptr_array(S)), n, _vp(ptr_array(ipiv)), _vp(info),
-                                     _vp(work), C.byref(lw), b, q.handle)
+    # the pointer arrays must outlive the call (a temporary's memory is reused at once)
+    dA, dP = ptr_array(S), ptr_array(ipiv)
+    rc = lib.magma_sgetrf_batched_tc(930, n, n, _vp(dA), n, _vp(dP), _vp(info), _vp(work), C.byref(lw),
+                                     b, q.handle)
     assert rc == 0
     assert lib.magma_sgetrf_batched_tc_status(n, n, _vp(work), b, q.handle) == 0
 
