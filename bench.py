@@ -1,8 +1,9 @@
 """Benchmark of the batched LU factor-and-solve path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dsgesv512|gesv32|vbatched4096|adjoint2048]
-                    [--profile [--batch B]]
+                    [--workload dsgesv512|gesv32|vbatched4096|adjoint2048|serve256]
+                    [--precision fp32|fp16|bf16] [--solver ir|gmres]
+                    [--profile [--batch B] [--eager]]
 
 Metric: FP64-accurate batched solves/s -- solves per second that meet the
 reference tester's accuracy bar ||b - A x||_inf / (||A||_inf ||x||_inf n eps)
@@ -363,11 +364,18 @@ class Dsgesv512:
     def accuracy(self, c, last):
         X = c["X"].transpose(1, 2)
         res = scaled_residuals(c["A"], X, c["Bm"])
-        it = c["iter"].cpu()
+        it = c["iter"].cpu().numpy()
+        kap = np.array(([1e2, 1e4, 1e6] * (self.batch // 3 + 1))[:self.batch])
+        per = {}
+        for kv in (1e2, 1e4, 1e6):
+            sel = it[kap == kv]
+            per[f"{kv:.0e}"] = {"iterations_histogram": {str(int(k)): int(v) for k, v in
+                                                          zip(*np.unique(sel, return_counts=True))},
+                                "fallbacks": int((sel < 0).sum())}
         return int((res <= 30).sum()), float(res.max()), {
             "iterations_histogram": {str(int(k)): int(v) for k, v in
-                                     zip(*np.unique(it.numpy(), return_counts=True))},
-            "fallbacks": int((it < 0).sum())}
+                                     zip(*np.unique(it, return_counts=True))},
+            "fallbacks": int((it < 0).sum()), "by_kappa": per}
 
     def fp64_path(self, c, steps, warmup):
         """Plain FP64 magma_dgesv_batched on the same inputs, private copies per step."""
@@ -547,7 +555,10 @@ class GesvVbatched:
             raise RuntimeError(f"magma_dgesv_vbatched_max_nocheck_work returned {rc}")
 
     def step(self, c, i):
-        c["graphs"][i].replay()
+        if getattr(self, "eager", False):         # --profile --eager: the same call, no graph
+            self._call(c, c["A"][i], c["B"][i], c["gq"])
+        else:
+            c["graphs"][i].replay()
 
     dominant_class = None        # graph replay: the step is the sort + the persistent kernel
     graph_kernels_per_step = 2
@@ -831,7 +842,10 @@ class Serve256:
         return c
 
     def step(self, c, i):
-        c["graph"].replay()
+        if getattr(self, "eager", False):         # --profile --eager: the same calls, no graph
+            self._calls(c, c["gq"])
+        else:
+            c["graph"].replay()
 
     def e2e_setup(self, c):
         import torch
@@ -966,8 +980,67 @@ class Serve256:
                                          f"dgetrf + dgetrs + transposed dgetrs + outer product)"
 
 
+class Routine:
+    """--profile only: one of the routines beside the LU path (Cholesky solve, batched
+    inverse, LU without pivoting, RBT solve) on `batch` FP64 matrices of order n with
+    4 right-hand sides, so that their kernels can be captured at a realistic size:
+    --workload posv|getri|gesv_nopiv|gesv_rbt [--batch B] (default 512 matrices,
+    n = 256)."""
+    n, nrhs = 256, 4
+
+    def __init__(self, name):
+        self.name = name
+        self.batch = 512
+
+    def setup(self, dev, nsteps, lib, q):
+        import torch
+        from magma_gb300.batched import ptr_array
+        g = torch.Generator(device="cpu").manual_seed(7)
+        b, n, r = self.batch, self.n, self.nrhs
+        A = torch.rand((b, n, n), generator=g, dtype=torch.float64) * 2 - 1
+        if self.name == "posv":
+            A = A @ A.transpose(1, 2) + n * torch.eye(n, dtype=torch.float64)
+        elif self.name == "gesv_nopiv":
+            A = A + n * torch.eye(n, dtype=torch.float64)     # diagonally dominant
+        S0 = A.transpose(1, 2).contiguous().to(dev)
+        B0 = (torch.rand((b, r, n), generator=g, dtype=torch.float64) * 2 - 1).to(dev)
+        c = {"lib": lib, "q": q, "S0": S0, "B0": B0, "S": S0.clone(), "B": B0.clone(),
+             "info": torch.empty((b,), dtype=torch.int32, device=dev)}
+        c["dS"], c["dB"] = ptr_array(c["S"]), ptr_array(c["B"])
+        if self.name == "getri":
+            c["inv"] = torch.empty_like(S0)
+            c["dI"] = ptr_array(c["inv"])
+            c["ipiv"] = torch.empty((b, n), dtype=torch.int32, device=dev)
+            c["dP"] = ptr_array(c["ipiv"])
+            rc = lib.magma_dgetrf_batched(n, n, vp(c["dS"]), n, vp(c["dP"]), vp(c["info"]), b, q.handle)
+            if rc != 0:
+                raise RuntimeError(f"magma_dgetrf_batched returned {rc}")
+        return c
+
+    def step(self, c, i):
+        lib, q, b, n, r = c["lib"], c["q"], self.batch, self.n, self.nrhs
+        if self.name != "getri":
+            c["S"].copy_(c["S0"])
+            c["B"].copy_(c["B0"])
+        if self.name == "posv":
+            rc = lib.magma_dposv_batched(122, n, r, vp(c["dS"]), n, vp(c["dB"]), n, vp(c["info"]), b,
+                                         q.handle)
+        elif self.name == "getri":
+            rc = lib.magma_dgetri_outofplace_batched(n, vp(c["dS"]), n, vp(c["dP"]), vp(c["dI"]), n,
+                                                     vp(c["info"]), b, q.handle)
+        elif self.name == "gesv_nopiv":
+            rc = lib.magma_dgesv_nopiv_batched(n, r, vp(c["dS"]), n, vp(c["dB"]), n, vp(c["info"]), b,
+                                               q.handle)
+        else:
+            rc = lib.magma_dgesv_rbt_batched(n, r, vp(c["dS"]), n, vp(c["dB"]), n, vp(c["info"]), b,
+                                             q.handle)
+        if rc != 0:
+            raise RuntimeError(f"{self.name} returned {rc}")
+
+
 WORKLOADS = {"dsgesv512": Dsgesv512, "gesv32": Gesv32, "vbatched4096": GesvVbatched,
              "adjoint2048": Adjoint2048, "serve256": Serve256}
+ROUTINES = ("posv", "getri", "gesv_nopiv", "gesv_rbt")
 
 
 # DRAM bytes (read + write) per unit of work of each workload's dominant kernel, from the ncu
@@ -1282,9 +1355,13 @@ def run_ours(args, wl):
         wl.step(c, i)
     torch.cuda.synchronize(dev)
     if args.profile:
+        # the steps inside an NVTX range "bench_step", so that a profiler can take
+        # only them (ncu --nvtx --nvtx-include "bench_step/")
         for k in range(args.steps):
+            torch.cuda.nvtx.range_push("bench_step")
             wl.step(c, args.warmup + k)
-        torch.cuda.synchronize(dev)
+            torch.cuda.synchronize(dev)
+            torch.cuda.nvtx.range_pop()
         return 0
 
     peaks = measured_peaks(stream.cuda_stream)
@@ -1401,7 +1478,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dsgesv512", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="dsgesv512", choices=sorted(WORKLOADS) + list(ROUTINES))
     ap.add_argument("--profile", action="store_true",
                     help="run warm-up and timed launches only (for ncu), print nothing")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16", "bf16"],
@@ -1411,7 +1488,16 @@ def main():
     ap.add_argument("--batch", type=int, default=None,
                     help="with --profile: run the workload on its first BATCH matrices "
                          "(a small case for full ncu captures)")
+    ap.add_argument("--eager", action="store_true",
+                    help="with --profile: call the graph-replayed workloads eagerly (for ncu)")
     args = ap.parse_args()
+    if args.workload in ROUTINES:
+        if not args.profile:
+            ap.error(f"--workload {args.workload} is only for --profile runs (kernel captures)")
+        wl = Routine(args.workload)
+        if args.batch is not None:
+            wl.batch = args.batch
+        return run_ours(args, wl)
     wl = WORKLOADS[args.workload]()
     if args.precision != "fp32":
         if args.workload != "dsgesv512":
@@ -1426,6 +1512,10 @@ def main():
         if not args.profile:
             ap.error("--batch is only for --profile runs")
         wl.batch = args.batch
+    if args.eager:
+        if not args.profile or args.workload not in ("vbatched4096", "serve256"):
+            ap.error("--eager is only for --profile runs of the graph-replayed workloads")
+        wl.eager = True
     if args.impl == "reference":
         return run_reference(args, wl)
     return run_ours(args, wl)

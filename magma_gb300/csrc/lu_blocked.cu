@@ -705,9 +705,14 @@ static bool outer_blocked(int m, int n)
 // 32-column panels with updates confined to the block, then one rank-128
 // update of everything right of it; the interchanges left of each panel after
 // the last step, as in the one-level form.
+// `outer`: the update right of each block (nullptr: the FP32 SIMT kernel,
+// outer_update); it is called with the block's first column J and `ctx`.
+typedef magma_int_t (*OuterUpdateFn)(int J, void *ctx);
+
 template <typename T>
 static magma_int_t blocked_getrf_outer(int m, int n, T **dA, int ldda, int **ipiv, int *info,
-                                       int batch, magma_queue_t q, StepSizes vs)
+                                       int batch, magma_queue_t q, StepSizes vs,
+                                       OuterUpdateFn outer = nullptr, void *ctx = nullptr)
 {
     const int mn = min(m, n);
     int panels = 0;
@@ -730,7 +735,7 @@ static magma_int_t blocked_getrf_outer(int m, int n, T **dA, int ldda, int **ipi
         }
         if constexpr (sizeof(T) == 4) {
             if (E < n || vs.m_arr) {
-                const magma_int_t rc = outer_update(m, n, J, dA, ldda, ipiv, vs, batch, q);
+                const magma_int_t rc = outer ? outer(J, ctx) : outer_update(m, n, J, dA, ldda, ipiv, vs, batch, q);
                 if (rc != 0) return rc;
             }
         }
@@ -765,6 +770,19 @@ magma_int_t blocked_getrf(int m, int n, T **dA, int ldda, int **ipiv, int *info,
                                     {nullptr, nullptr, nullptr}, q->stream);
     return MAGMA_SUCCESS;
 }
+
+// The two-level FP32 factorisation with a caller-provided update right of each
+// block (the tensor-core form, lu_tc.cu), for uniform batches that
+// outer_blocked() accepts; MAGMA_ERR_NOT_SUPPORTED otherwise.
+magma_int_t blocked_getrf_two_level(int m, int n, float **dA, int ldda, int **ipiv, int *info,
+                                    int batch, magma_queue_t q, OuterUpdateFn outer, void *ctx)
+{
+    if (batch <= 0 || m == 0 || n == 0) return MAGMA_SUCCESS;
+    if (!outer_blocked<float>(m, n)) return MAGMA_ERR_NOT_SUPPORTED;
+    return blocked_getrf_outer<float>(m, n, dA, ldda, ipiv, info, batch, q, {nullptr, nullptr, nullptr},
+                                      outer, ctx);
+}
+bool two_level_applies(int m, int n) { return outer_blocked<float>(m, n); }
 
 template int blocked_panel_width<float>(int, int, int);
 template magma_int_t blocked_getrf_steps<float>(int, int, float **, int, int **, int *, int,

@@ -33,6 +33,8 @@
 #include "common.cuh"
 #include "trace.cuh"
 #include "lu_core.cuh"
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 namespace mlu {
 
@@ -148,8 +150,21 @@ __device__ __forceinline__ void ob_stage(float *dst, const float *A, size_t ld, 
     cp_async_commit();
 }
 
+template <typename H> __device__ __forceinline__ H ob_to_half(float x);
+template <> __device__ __forceinline__ float ob_to_half<float>(float x) { return x; }
+template <> __device__ __forceinline__ __nv_bfloat16 ob_to_half<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
+template <> __device__ __forceinline__ __half ob_to_half<__half>(float x) { return __float2half_rn(x); }
+
+// TC = false: the whole update on the FP32 pipes (steps 1-4 above).
+// TC = true (the tensor-core forms, lu_tc.cu): steps 1-3 and 5 only, plus
+// what the tensor-core update needs to run in place afterwards -- the rows
+// below the block that receive an original top row get it now, and U12 is
+// rounded to H into the staging rows Ub[mat][column - E][0..128) (K-major,
+// zero for k >= K), upad rows per matrix.
+template <bool TC, typename H>
 __global__ void __launch_bounds__(OB_THREADS, 2)
-outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_array, StepSizes vs)
+outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_array, StepSizes vs,
+                    H *Ub, int upad)
 {
     extern __shared__ __align__(16) float ob_smem[];
     float *sU = ob_smem;                          // [OUTER_NB][OB_TN], swizzled (ob_uidx)
@@ -159,6 +174,7 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
     __shared__ unsigned s_dmask[OB_MAX_ROWS / 32];   // rows below the block that receive a top row
     __shared__ int s_dsrc[OUTER_NB];                 // ... and which (listed per interchange)
     __shared__ unsigned char s_didx[OB_MAX_ROWS];    // row - E -> index into s_dsrc
+    __shared__ int s_drow[TC ? OUTER_NB : 1];        // (TC) the row of entry e, row - E
     __shared__ int s_nt;
     const int mat = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int K = OUTER_NB;
@@ -190,6 +206,7 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
             const int row = s_piv[k] - E;
             s_dsrc[e] = ob_resolve(s_piv[k], J, K, s_piv);
             s_didx[row] = (unsigned char)e;
+            if (TC) s_drow[TC ? e : 0] = row;
             atomicOr(&s_dmask[row >> 5], 1u << (row & 31));
         }
     }
@@ -284,7 +301,7 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
     //    OB_RING stages of OB_SK columns, continuous across the row tiles: stage
     //    g holds columns J + OB_SK (g mod nsk) of tile g / nsk and is issued
     //    OB_RING - 1 stages ahead; one barrier per stage.
-    const int below = m - E;
+    const int below = TC ? 0 : m - E;             // TC: the tensor cores update A22
     const int ntiles = below > 0 ? (below + OB_TM - 1) / OB_TM : 0;
     const int nsk = (K + OB_SK - 1) / OB_SK;       // stages per tile
     const int nst = ntiles * nsk;
@@ -399,6 +416,24 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
     }
     cp_async_wait<0>();
 
+    if constexpr (TC) {
+        // rows below that receive an original top row take it now (the top rows
+        // are still original); then U12 rounded to H for the tensor cores
+        const int nt = s_nt;
+        for (int x = tid; x < nt * w; x += OB_THREADS) {
+            const int e = x % nt, c = x / nt;
+            float *colp = A + (size_t)(c0 + c) * ld;
+            colp[E + s_drow[e]] = colp[s_dsrc[e]];
+        }
+        H *U = Ub + (size_t)mat * upad * OUTER_NB + (size_t)(c0 - E) * OUTER_NB;
+#pragma unroll 4
+        for (int u = 0; u < OB_U_FLOATS / OB_THREADS; u++) {
+            const int idx = tid + u * OB_THREADS, k = idx & (OUTER_NB - 1), c = idx / OUTER_NB;
+            if (c < w) U[(size_t)c * OUTER_NB + k] = ob_to_half<H>(k < K ? sU[ob_uidx(k, c)] : 0.f);
+        }
+        __syncthreads();                          // the copies read top rows that step 5 rewrites
+    }
+
     // 5. U12 into the block's top rows of the tile (read by no other CTA)
 #pragma unroll 4
     for (int u = 0; u < OB_U_FLOATS / OB_THREADS; u++) {
@@ -415,7 +450,8 @@ magma_int_t outer_update(int m, int n, int J, float **dA, int ldda, int **ipiv, 
                          int batch, magma_queue_t q)
 {
     static size_t dyn[MLU_MAX_DEVICES];
-    if (mlu_device_cached(dyn, [] { return mlu_allow_dynamic_smem(outer_update_kernel); }) < OB_SMEM)
+    if (mlu_device_cached(dyn, [] { return mlu_allow_dynamic_smem(outer_update_kernel<false, float>); }) <
+        OB_SMEM)
         return MAGMA_ERR_NOT_SUPPORTED;
     const int K = min(OUTER_NB, min(m, n) - J);
     // a variable-size batch: a matrix whose block is narrower starts its tiles earlier
@@ -431,11 +467,39 @@ magma_int_t outer_update(int m, int n, int J, float **dA, int ldda, int **ipiv, 
             v.n_arr += b0;
             v.ld_arr += b0;
         }
-        MLU_LAUNCH(mlu::KC_OUTER, s, outer_update_kernel<<<dim3(tiles, nb), OB_THREADS, OB_SMEM, s>>>(
-            m, n, J, dA + b0, ldda, ipiv ? ipiv + b0 : nullptr, v));
+        MLU_LAUNCH(mlu::KC_OUTER, s, outer_update_kernel<false, float><<<dim3(tiles, nb), OB_THREADS, OB_SMEM, s>>>(
+            m, n, J, dA + b0, ldda, ipiv ? ipiv + b0 : nullptr, v, nullptr, 0));
     }
     MLU_CHECK_LAUNCH();
     return MAGMA_SUCCESS;
 }
+
+// Steps 1-3 of the update right of block J for the tensor-core forms, uniform
+// batch of m x n matrices: the interchanges (rows below applied in place), U12
+// in place, and U12 rounded to H into Ub ([batch][upad][128]).
+template <typename H>
+magma_int_t outer_prep_tc(int m, int n, int J, float **dA, int ldda, int **ipiv, int batch, H *Ub,
+                          int upad, magma_queue_t q)
+{
+    static size_t dyn[MLU_MAX_DEVICES];
+    if (mlu_device_cached(dyn, [] { return mlu_allow_dynamic_smem(outer_update_kernel<true, H>); }) < OB_SMEM)
+        return MAGMA_ERR_NOT_SUPPORTED;
+    const int K = min(OUTER_NB, min(m, n) - J);
+    if (K <= 0 || J + K >= n) return MAGMA_SUCCESS;
+    const int tiles = (n - J - K + OB_TN - 1) / OB_TN;
+    cudaStream_t s = q->stream;
+    for (int b0 = 0; b0 < batch; b0 += MLU_MAX_GRID_Y) {
+        const int nb = min(batch - b0, (int)MLU_MAX_GRID_Y);
+        MLU_LAUNCH(mlu::KC_OUTER, s, outer_update_kernel<true, H><<<dim3(tiles, nb), OB_THREADS, OB_SMEM, s>>>(
+            m, n, J, dA + b0, ldda, ipiv ? ipiv + b0 : nullptr, StepSizes{nullptr, nullptr, nullptr},
+            Ub + (size_t)b0 * upad * OUTER_NB, upad));
+    }
+    MLU_CHECK_LAUNCH();
+    return MAGMA_SUCCESS;
+}
+template magma_int_t outer_prep_tc<__nv_bfloat16>(int, int, int, float **, int, int **, int, __nv_bfloat16 *,
+                                                  int, magma_queue_t);
+template magma_int_t outer_prep_tc<__half>(int, int, int, float **, int, int **, int, __half *, int,
+                                           magma_queue_t);
 
 }  // namespace mlu

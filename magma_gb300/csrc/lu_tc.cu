@@ -19,6 +19,18 @@
 //                     warps read D back with tcgen05.ld and add it to A22.
 // Smaller trailing blocks use the FP32 SIMT tile of the plain path.
 //
+// For matrices the two-level blocking serves (at most 1024 rows, columns right
+// of a first 128-column block; lu_blocked.cu, lu_outer.cu) the update is done
+// once per 128-column block instead, with K = 128:
+//   outer_update_kernel<true, H>  (lu_outer.cu) the block's interchanges and
+//                     U12 = L11^{-1} A12 in FP32, in place, and U12 rounded
+//                     to H into the staging buffer Ub[batch][row][128];
+//   tc_stage_l21_kernel  L21 rounded to H into Lb[batch][row][128];
+//   tc_gemm128_kernel  one CTA per 128x128 tile of A22: TMA brings the four
+//                     32-deep slices of both operands (64 KB), one thread
+//                     issues eight tcgen05.mma kind::f16 (K = 16 each) into
+//                     one TMEM accumulator, and four warps add it to A22.
+//
 // Every wait on an mbarrier is bounded: on timeout the CTA records an error
 // in a device flag (the host returns MAGMA_ERR_UNKNOWN), waits once more for
 // its own copies, frees its tensor memory and exits.
@@ -28,6 +40,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <type_traits>
 
 namespace mlu {
 
@@ -245,6 +258,141 @@ tc_update_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant_
 }
 
 // ---------------------------------------------------------------------------
+// Two-level form.  Lb[mat][i][k] = rnd(L(E + i, J + k)) for i < m - E, k < 128
+// (zero for k >= K).  One CTA per (matrix, 32 rows): coalesced reads down the
+// columns of L21 into shared memory, then rows of 128 k written as pairs.
+constexpr int TC_KB = 128;                           // k of the two-level update
+template <typename H2, typename H>
+__global__ void __launch_bounds__(256)
+tc_stage_l21_kernel(int m, int J, int K, float **dA_array, int ldda, H *Lb, int pad)
+{
+    __shared__ float t[TC_KB][33];
+    const int mat = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int E = J + K, r0 = E + blockIdx.x * 32;
+    const float *A = dA_array[mat];
+    for (int k = warp; k < TC_KB; k += 8)
+        t[k][lane] = (k < K && r0 + lane < m) ? A[r0 + lane + (size_t)(J + k) * ldda] : 0.f;
+    __syncthreads();
+    H *L = Lb + (size_t)mat * pad * TC_KB + (size_t)(r0 - E) * TC_KB;
+    for (int x = tid; x < 32 * TC_KB / 2; x += 256) {
+        const int row = x / (TC_KB / 2), kp = x % (TC_KB / 2);
+        if (r0 + row < m) {
+            H2 v;
+            v.x = to_half<H>(t[2 * kp][row]);
+            v.y = to_half<H>(t[2 * kp + 1][row]);
+            *reinterpret_cast<H2 *>(L + (size_t)row * TC_KB + 2 * kp) = v;
+        }
+    }
+}
+
+// One 128x128 tile of A22 (rows and columns from E) += -(L21 U12) with K = 128:
+// TMA loads the four 32-deep slices of each operand (64-byte swizzle, 8 KB
+// each), one thread issues the eight MMAs, four warps read TMEM back and add.
+template <bool BF16>
+__global__ void __launch_bounds__(128, 1)
+tc_gemm128_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmU,
+                  float **dA_array, int ldda, int m, int n, int E, int tiles_m, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ __align__(8) uint64_t bar_tma, bar_mma;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_ok;
+    unsigned char *sbase = (unsigned char *)(((uintptr_t)tc_smem + 1023) & ~(uintptr_t)1023);
+    unsigned char *sL = sbase, *sU = sbase + (TC_KB / TC_K) * TC_TILE_BYTES;   // 32 KB each
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int mat = blockIdx.y;
+    const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_u32(&tmem_base)), "r"(TC_N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(&bar_tma, 1);
+        mbar_init(&bar_mma, 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+
+    if (tid == 0) {
+        mbar_expect_tx(&bar_tma, 2 * (TC_KB / TC_K) * TC_TILE_BYTES);
+#pragma unroll
+        for (int c = 0; c < TC_KB / TC_K; c++) {
+            tma_load_3d(sL + c * TC_TILE_BYTES, &tmL, c * TC_K, tm * TC_M, mat, &bar_tma);
+            tma_load_3d(sU + c * TC_TILE_BYTES, &tmU, c * TC_K, tn * TC_N, mat, &bar_tma);
+        }
+        int ok = mbar_wait(&bar_tma, 0);
+        if (ok) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t idesc = f16_idesc(BF16);
+            const uint32_t aL = smem_u32(sL), aU = smem_u32(sU);
+#pragma unroll
+            for (int s = 0; s < TC_KB / 16; s++) {
+                const uint32_t off = (s >> 1) * TC_TILE_BYTES + (s & 1) * 32;
+                const uint64_t da = kmajor_sw64_desc(aL + off);
+                const uint64_t db = kmajor_sw64_desc(aU + off);
+                const uint32_t acc = s > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                    ::"r"(tmem), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(smem_u32(&bar_mma)) : "memory");
+        } else {
+            atomicExch(err, 1);
+            mbar_wait(&bar_tma, 0);          // give the copies in flight one more chance
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    const bool ok = s_ok && mbar_wait(&bar_mma, 0);
+    if (s_ok && !ok && lane == 0) atomicExch(err, 2);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (ok) {
+        // warp w reads TMEM lanes 32w..32w+31: thread = one row of the tile
+        float *A = dA_array[mat];
+        const int r = E + tm * TC_M + warp * 32 + lane;
+        const int cbase = E + tn * TC_N;
+#pragma unroll 1
+        for (int cc = 0; cc < TC_N; cc += 16) {
+            float a[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int c = cbase + cc + j;
+                a[j] = (r < m && c < n) ? A[r + (size_t)c * ldda] : 0.f;
+            }
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                  "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+                  "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                : "r"(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (r < m) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int c = cbase + cc + j;
+                    if (c < n) A[r + (size_t)c * ldda] = a[j] + __uint_as_float(v[j]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N));
+}
+
+// ---------------------------------------------------------------------------
 // Self-test of the bounded waits: one CTA takes tensor memory as the update
 // kernel does, then waits on an mbarrier that nothing arrives at (no copy and
 // no MMA is ever issued, so nothing is in flight when the wait gives up).  The
@@ -299,13 +447,14 @@ static EncodeTiledFn encode_fn()
     return fn;
 }
 
-// 3-D map over a staging buffer [batch][pad][32] of 16-bit values, box 32 x 128 x 1.
-static bool make_map(CUtensorMap *map, void *base, int pad, int batch, bool bf16)
+// 3-D map over a staging buffer [batch][pad][kdim] of 16-bit values (kdim 32
+// or 128), box 32 x 128 x 1: one 32-deep slice of a 128-row operand tile.
+static bool make_map(CUtensorMap *map, void *base, int pad, int batch, bool bf16, int kdim = TC_K)
 {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
-    const cuuint64_t dims[3] = {(cuuint64_t)TC_K, (cuuint64_t)pad, (cuuint64_t)batch};
-    const cuuint64_t strides[2] = {(cuuint64_t)TC_K * 2, (cuuint64_t)pad * TC_K * 2};
+    const cuuint64_t dims[3] = {(cuuint64_t)kdim, (cuuint64_t)pad, (cuuint64_t)batch};
+    const cuuint64_t strides[2] = {(cuuint64_t)kdim * 2, (cuuint64_t)pad * kdim * 2};
     const cuuint32_t box[3] = {(cuuint32_t)TC_K, (cuuint32_t)TC_M, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r = fn(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16,
@@ -324,7 +473,8 @@ static TcLayout tc_layout(int m, int n, int batch)
 {
     TcLayout L;
     L.pad = ((max(m, n) + TC_M - 1) / TC_M) * TC_M;
-    const size_t half_bytes = (size_t)batch * L.pad * TC_K * 2;
+    // rows of 128 k (the two-level form); the one-level form uses the first 32
+    const size_t half_bytes = (size_t)batch * L.pad * TC_KB * 2;
     L.lb = 0;
     L.ub = (half_bytes + 1023) & ~(size_t)1023;
     L.err = L.ub + ((half_bytes + 1023) & ~(size_t)1023);
@@ -345,15 +495,74 @@ magma_int_t blocked_getrf_steps(int m, int n, T **dA, int ldda, int **ipiv, int 
                                 magma_queue_t q, int j0, int ib, bool update);
 template <typename T>
 int blocked_panel_width(int m, int n, int j0);
+typedef magma_int_t (*OuterUpdateFn)(int J, void *ctx);
+magma_int_t blocked_getrf_two_level(int m, int n, float **dA, int ldda, int **ipiv, int *info,
+                                    int batch, magma_queue_t q, OuterUpdateFn outer, void *ctx);
+bool two_level_applies(int m, int n);
+template <typename H>
+magma_int_t outer_prep_tc(int m, int n, int J, float **dA, int ldda, int **ipiv, int batch, H *Ub,
+                          int upad, magma_queue_t q);
 }
 
 namespace mlu {
+
+// Arguments of the two-level form's update right of a block.
+template <typename H>
+struct TcOuterCtx {
+    int m, n, ldda, batch, pad;
+    float **dA;
+    int **ipiv;
+    H *Lb, *Ub;
+    int *err;
+    CUtensorMap mapL, mapU;
+    magma_queue_t q;
+};
+
+template <typename H, bool BF16>
+static magma_int_t tc_outer_update(int J, void *vctx)
+{
+    TcOuterCtx<H> &c = *static_cast<TcOuterCtx<H> *>(vctx);
+    const int K = min(TC_KB, min(c.m, c.n) - J), E = J + K;
+    magma_int_t rc = outer_prep_tc<H>(c.m, c.n, J, c.dA, c.ldda, c.ipiv, c.batch, c.Ub, c.pad, c.q);
+    if (rc != 0 || E >= c.m) return rc;             // no rows below the block: U12 was all
+    using H2 = typename std::conditional<BF16, __nv_bfloat162, __half2>::type;
+    const int rm = c.m - E, rn = c.n - E;
+    const int tiles_m = (rm + TC_M - 1) / TC_M, tiles_n = (rn + TC_N - 1) / TC_N;
+    cudaStream_t s = c.q->stream;
+    MLU_LAUNCH(mlu::KC_OTHER, s, tc_stage_l21_kernel<H2, H><<<dim3((rm + 31) / 32, c.batch), 256, 0, s>>>(
+        c.m, J, K, c.dA, c.ldda, c.Lb, c.pad));
+    // 2 x 32 KB of operands + alignment, requested as 66 KB so that at most three
+    // CTAs share an SM: three 128-column accumulators within its 512 TMEM columns
+    MLU_LAUNCH(mlu::KC_TC_UPDATE, s, tc_gemm128_kernel<BF16><<<dim3(tiles_m * tiles_n, c.batch), 128, 66 * 1024, s>>>(
+        c.mapL, c.mapU, c.dA, c.ldda, c.m, c.n, E, tiles_m, c.err));
+    MLU_CHECK_LAUNCH();
+    return MAGMA_SUCCESS;
+}
 
 template <typename H, bool BF16>
 static magma_int_t tc_getrf(int m, int n, float **dA, int ldda, int **ipiv, int *info, int batch,
                             void *work, magma_queue_t q)
 {
     const TcLayout L = tc_layout(m, n, batch);
+    if (two_level_applies(m, n) && batch <= MLU_MAX_GRID_Y) {
+        // 128-column blocks, one K = 128 tensor-core update right of each
+        char *w = (char *)work;
+        TcOuterCtx<H> c;
+        c.m = m; c.n = n; c.ldda = ldda; c.batch = batch; c.pad = L.pad;
+        c.dA = dA; c.ipiv = ipiv; c.q = q;
+        c.Lb = (H *)(w + L.lb);
+        c.Ub = (H *)(w + L.ub);
+        c.err = (int *)(w + L.err);
+        if (!make_map(&c.mapL, c.Lb, L.pad, batch, BF16, TC_KB) ||
+            !make_map(&c.mapU, c.Ub, L.pad, batch, BF16, TC_KB))
+            return MAGMA_ERR_NOT_SUPPORTED;
+        static size_t dyn_cache[MLU_MAX_DEVICES];
+        if (mlu_device_cached(dyn_cache, [] { return mlu_allow_dynamic_smem(tc_gemm128_kernel<BF16>); }) <
+            66 * 1024)
+            return MAGMA_ERR_NOT_SUPPORTED;
+        cudaMemsetAsync(c.err, 0, sizeof(int), q->stream);
+        return blocked_getrf_two_level(m, n, dA, ldda, ipiv, info, batch, q, tc_outer_update<H, BF16>, &c);
+    }
     char *w = (char *)work;
     H *Lb = (H *)(w + L.lb);
     H *Ub = (H *)(w + L.ub);

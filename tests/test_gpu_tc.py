@@ -1,15 +1,18 @@
 """Tensor-core trailing update (tcgen05 + TMEM, TMA-fed) of the FP32
 factorisation, magma_sgetrf_batched_tc.
 
-Exactness test: A = [[I, U12], [L21, A22]] with L21 and U12 multiples of 1/8
-in (-1, 1) -- exactly representable in BF16 and FP16 -- and A22 multiples of
-1/64 makes the first panel pivot-free with L21 as multipliers and U12
-unchanged, and every partial sum of the first trailing update exact in FP32.  That update is the only one large
-enough for the tensor cores (128 x 128 tiles); everything after it runs on the
-FP32 kernels.  So the result must equal the FP32 SIMT factorisation bit for
-bit -- which checks the TMA maps, the swizzled operand descriptors, the MMA
-instruction descriptor (including the negated A), the TMEM read-back and the
-tile indexing.  Then a random-matrix test bounds the backward error."""
+Exactness test: A = [[I, U12], [L21, A22]] with I of order 128 (one block of
+the two-level factorisation), L21 and U12 multiples of 1/8 in (-1, 1) --
+exactly representable in BF16 and FP16 -- and A22 multiples of 1/64 makes the
+first 128 columns pivot-free with L21 as multipliers and U12 unchanged, and
+every partial sum of the rank-128 tensor-core update exact in FP32.
+Everything else (the panels, the updates inside a block, the U12 solves) runs
+on the FP32 kernels.  So the result must equal the FP32 SIMT factorisation bit
+for bit -- which checks the TMA maps, the swizzled operand descriptors of the
+four 32-deep slices, the MMA instruction descriptor (including the negated A),
+the TMEM read-back, the tile indexing, and the rows below the block that the
+interchange step moves in place.  Then a random-matrix test bounds the
+backward error."""
 import ctypes as C
 
 import numpy as np
@@ -48,13 +51,13 @@ def _tc_getrf(S, m, prec, cuda):
     return ipiv, info
 
 
-def _structured(rng, batch, m, n):
+def _structured(rng, batch, m, n, w=128):
     # A22 in multiples of 1/64 too: every partial sum of the first update is then
     # exact in FP32, whichever order the FP32 or the tensor-core path adds in
     A = (rng.integers(-63, 64, (batch, m, n)) / 64.0).astype(np.float32)
-    A[:, :32, :32] = np.eye(32, dtype=np.float32)
-    A[:, 32:, :32] = rng.integers(-7, 8, (batch, m - 32, 32)) / 8.0     # L21, |l| < 1
-    A[:, :32, 32:] = rng.integers(-7, 8, (batch, 32, n - 32)) / 8.0     # U12
+    A[:, :w, :w] = np.eye(w, dtype=np.float32)
+    A[:, w:, :w] = rng.integers(-7, 8, (batch, m - w, w)) / 8.0     # L21, |l| < 1
+    A[:, :w, w:] = rng.integers(-7, 8, (batch, w, n - w)) / 8.0     # U12
     return A
 
 
