@@ -761,6 +761,45 @@ magma_int_t magma_dvbatched_tuning_set(const magma_int_t *nb, const magma_int_t 
 magma_int_t magma_svbatched_tuning_set(const magma_int_t *nb, const magma_int_t *tile);
 
 /* ------------------------------------------------------------------------
+ * Tuning of the fixed-size factorisation and the tuning file.  No counterpart
+ * in the reference, whose batched LU reads fixed crossover tables
+ * (control/get_batched_crossover.cpp:300-342, 918-928;
+ * control/get_batched_gemm_decision.cpp:233-253).  One table per precision,
+ * six size bins of max(m, n): <= 64, 128, 256, 512, 1024, larger.  Entries:
+ *   two_level[b]  FP32: 1 = 128-column blocks with one rank-128 update right of
+ *                 each, 0 = a rank-32 update after every 32-column panel;
+ *   band_ctas[b]  FP32: the fused band kernel when a step gives at least this
+ *                 many CTAs per SM (1, 2 or 4);
+ *   tile64[b]     FP64: 1 = 64 x 64 update tiles, 0 = 32 x 32.
+ * Every setting gives bit-identical results; only the time changes.
+ *
+ * magma_?getrf_batched_autotune: times the candidates of every bin up to max_n
+ * on `batch` trial matrices on `queue`'s device (allocates them, synchronises)
+ * and installs the fastest.  Must not run beside other calls of this library.
+ * Errors: -1 max_n < 0, -2 batch < 1, -3 no queue, MAGMA_ERR_DEVICE_ALLOC.
+ * magma_?getrf_batched_tuning_get / _set: read or replace the table (six
+ * entries per array); _set returns -1 / -2 / -3 for a bad entry.
+ *
+ * magma_lu_tuning_save / _load: write or read this table and the
+ * variable-size one (magma_?vbatched_tuning_*) as a JSON file; _load checks
+ * the whole file before installing anything.  A queue created while the
+ * environment variable MAGMA_LU_TUNING_FILE names a file loads it, once per
+ * process.  Return 0, -1 for a NULL path, MAGMA_ERR_UNKNOWN for an unreadable
+ * or malformed file. */
+magma_int_t magma_dgetrf_batched_autotune(magma_int_t max_n, magma_int_t batch, magma_queue_t queue);
+magma_int_t magma_sgetrf_batched_autotune(magma_int_t max_n, magma_int_t batch, magma_queue_t queue);
+magma_int_t magma_dgetrf_batched_tuning_get(magma_int_t *two_level, magma_int_t *band_ctas,
+                                            magma_int_t *tile64);
+magma_int_t magma_sgetrf_batched_tuning_get(magma_int_t *two_level, magma_int_t *band_ctas,
+                                            magma_int_t *tile64);
+magma_int_t magma_dgetrf_batched_tuning_set(const magma_int_t *two_level, const magma_int_t *band_ctas,
+                                            const magma_int_t *tile64);
+magma_int_t magma_sgetrf_batched_tuning_set(const magma_int_t *two_level, const magma_int_t *band_ctas,
+                                            const magma_int_t *tile64);
+magma_int_t magma_lu_tuning_save(const char *path);
+magma_int_t magma_lu_tuning_load(const char *path);
+
+/* ------------------------------------------------------------------------
  * Launch accounting and kernel timing.  No counterpart in the reference,
  * whose testers time whole calls on the host
  * (testing/testing_zgesv_batched.cpp:158-166).

@@ -453,3 +453,45 @@ def autotune_vbatched(max_n: int, dtype: torch.dtype = torch.float64,
         int(max_n), nb, tile, q.handle)
     _check(rc, "getrf_vbatched_autotune")
     return _tune_dict(nb, tile)
+
+
+# fixed-size factorisation tuning (magma_?getrf_batched_autotune / _tuning_get / _set) and
+# the tuning file (magma_lu_tuning_save / _load)
+FIXED_TUNE_BINS = ("<=64", "<=128", "<=256", "<=512", "<=1024", ">1024")
+
+
+def getrf_batched_tuning(dtype: torch.dtype = torch.float32) -> dict:
+    """The fixed-size table of one precision: {bin: {two_level, band_ctas, tile64}}."""
+    a, b, c = (C.c_int * 6)(), (C.c_int * 6)(), (C.c_int * 6)()
+    rc = getattr(_L.load(), f"magma_{_tune_prefix(dtype)}getrf_batched_tuning_get")(a, b, c)
+    _check(rc, "getrf_batched_tuning_get")
+    return {k: {"two_level": a[i], "band_ctas": b[i], "tile64": c[i]}
+            for i, k in enumerate(FIXED_TUNE_BINS)}
+
+
+def set_getrf_batched_tuning(two_level, band_ctas, tile64, dtype: torch.dtype = torch.float32) -> None:
+    arr = lambda v: (C.c_int * 6)(*[int(x) for x in v])
+    rc = getattr(_L.load(), f"magma_{_tune_prefix(dtype)}getrf_batched_tuning_set")(
+        arr(two_level), arr(band_ctas), arr(tile64))
+    _check(rc, "getrf_batched_tuning_set")
+
+
+def autotune_getrf_batched(max_n: int, batch: int, dtype: torch.dtype = torch.float32,
+                           queue: Queue | None = None) -> dict:
+    """Time the fixed-size candidates of every bin up to max_n on `batch` trial matrices and
+    install the fastest (magma_?getrf_batched_autotune).  Returns the table."""
+    q = queue or Queue.current()
+    rc = getattr(_L.load(), f"magma_{_tune_prefix(dtype)}getrf_batched_autotune")(
+        int(max_n), int(batch), q.handle)
+    _check(rc, "getrf_batched_autotune")
+    return getrf_batched_tuning(dtype)
+
+
+def save_tuning(path) -> None:
+    """Write both precisions' fixed-size and variable-size tables as JSON."""
+    _check(_L.load().magma_lu_tuning_save(str(path).encode()), "magma_lu_tuning_save")
+
+
+def load_tuning(path) -> None:
+    """Install the tables of a file written by save_tuning (checked as a whole first)."""
+    _check(_L.load().magma_lu_tuning_load(str(path).encode()), "magma_lu_tuning_load")

@@ -156,6 +156,24 @@ static inline size_t mlu_device_cached(size_t *cache, F f)
 }
 
 namespace mlu {
+// Tuning of the fixed-size factorisation (tuning.cu): per precision and size bin
+// of max(m, n) (<= 64, 128, 256, 512, 1024, larger).
+constexpr int FIXED_TUNE_BINS = 6;
+struct FixedTune {
+    unsigned char two_level[FIXED_TUNE_BINS];   // FP32: 128-column blocks (lu_outer.cu)
+    unsigned char band_ctas[FIXED_TUNE_BINS];   // FP32: fused band kernel from this many CTAs per SM
+    unsigned char tile64[FIXED_TUNE_BINS];      // FP64: 64 x 64 update tiles (else 32 x 32)
+};
+struct FixedChoice {
+    bool two_level;
+    int band_ctas;
+    bool tile64;
+};
+FixedChoice fixed_choice(bool fp64, int m, int n);
+int fixed_tune_bin(int m, int n);
+// loads the tuning file named by MAGMA_LU_TUNING_FILE, once per process
+void tuning_load_env_once();
+
 // Every device allocation the library makes for itself (queue workspaces, the
 // autotuner's trial batches) goes through this wrapper, so that a test can make
 // the next allocations fail (magma_lu_fail_allocations) and check the

@@ -594,6 +594,7 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
         if (band_used<T>()) mlu_allow_dynamic_smem(band_kernel);
         return v;
     });
+    const FixedChoice tune = fixed_choice(sizeof(T) == 8, m, n);
     const int pm = m - j0;
     const int rpt = panel_rows_per_thread<T>(pm);
     const size_t smem = rpt == 1   ? panel_regs_smem_bytes<T, 1>()
@@ -623,7 +624,7 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
         const int rm = m - j0 - ib, rn = block_col_end(bj, m, n) - j0 - ib;
         const int bands = rn > 0 ? (rn + BAND_N - 1) / BAND_N : 0;
         const bool fused = band_used<T>() && update && bands > 0 &&
-                           (long long)bands * nb >= 2LL * mlu_sm_count();
+                           (long long)bands * nb >= (long long)tune.band_ctas * mlu_sm_count();
         const int ncl = defer_left ? 0 : (j0 + SWAP_COLS - 1) / SWAP_COLS;
         const int ncr = fused ? 0 : (rn + SWAP_COLS - 1) / SWAP_COLS;
         if (ncl + ncr > 0)
@@ -633,7 +634,7 @@ magma_int_t blocked_getrf_steps_l(int m, int n, T **dA, int ldda, int **ipiv, in
             MLU_LAUNCH(mlu::KC_GEMM, s, band_kernel<<<dim3(bands, nb), BAND_THREADS, band_smem_bytes(), s>>>(
                 m, n, j0, ib, reinterpret_cast<float **>(dAb), ldda, ipb, vs, bj));
         } else if (update && rm > 0 && rn > 0) {
-            if (rm <= 32 || rn <= 32) {
+            if (!tune.tile64 || rm <= 32 || rn <= 32) {
                 // a thin trailing block: 32 x 32 tiles, so that no FMA of a
                 // 64 x 64 tile runs on padding (each costs full FP64 issue slots)
                 const int tiles_m = (rm + 31) / 32, tiles_n = (rn + 31) / 32;
@@ -695,10 +696,16 @@ magma_int_t outer_update(int m, int n, int J, float **dA, int ldda, int **ipiv, 
 // The two-level blocking (lu_outer.cu) serves FP32 matrices of at most
 // LEFT_DEFER_MAX_M rows (register panels of width 32, interchanges left of the
 // panels deferred) with columns right of a first block.
+// (and the tuning table chooses it for the size: tuning.cu)
+template <typename T>
+static bool outer_blocked_shape(int m, int n)
+{
+    return sizeof(T) == 4 && m <= LEFT_DEFER_MAX_M && n > OUTER_NB && min(m, n) > PANEL_NB;
+}
 template <typename T>
 static bool outer_blocked(int m, int n)
 {
-    return sizeof(T) == 4 && m <= LEFT_DEFER_MAX_M && n > OUTER_NB && min(m, n) > PANEL_NB;
+    return outer_blocked_shape<T>(m, n) && fixed_choice(false, m, n).two_level;
 }
 
 // Steps of the two-level blocked factorisation: per 128-column block, its
@@ -783,6 +790,7 @@ magma_int_t blocked_getrf_two_level(int m, int n, float **dA, int ldda, int **ip
                                       outer, ctx);
 }
 bool two_level_applies(int m, int n) { return outer_blocked<float>(m, n); }
+bool two_level_possible(int m, int n) { return outer_blocked_shape<float>(m, n); }
 
 template int blocked_panel_width<float>(int, int, int);
 template magma_int_t blocked_getrf_steps<float>(int, int, float **, int, int **, int *, int,

@@ -360,13 +360,23 @@ tc_gemm128_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant
         float *A = dA_array[mat];
         const int r = E + tm * TC_M + warp * 32 + lane;
         const int cbase = E + tn * TC_N;
+        // the next chunk's 16 elements of A22 are loaded before this chunk is added
+        float a[16], an[16];
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            const int c = cbase + j;
+            an[j] = (r < m && c < n) ? A[r + (size_t)c * ldda] : 0.f;
+        }
 #pragma unroll 1
         for (int cc = 0; cc < TC_N; cc += 16) {
-            float a[16];
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int c = cbase + cc + j;
-                a[j] = (r < m && c < n) ? A[r + (size_t)c * ldda] : 0.f;
+            for (int j = 0; j < 16; j++) a[j] = an[j];
+            if (cc + 16 < TC_N) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int c = cbase + cc + 16 + j;
+                    an[j] = (r < m && c < n) ? A[r + (size_t)c * ldda] : 0.f;
+                }
             }
             uint32_t v[16];
             asm volatile(

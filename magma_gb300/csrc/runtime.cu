@@ -55,6 +55,7 @@ extern "C" void magma_xerbla(const char *name, magma_int_t info) {
 
 extern "C" void magma_queue_create_internal(magma_device_t device, magma_queue_t *queue_ptr,
                                             const char *, const char *, int) {
+    mlu::tuning_load_env_once();
     magma_queue_t q = (magma_queue_t)calloc(1, sizeof(struct magma_queue));
     if (!q) { *queue_ptr = nullptr; return; }
     q->device = device;
@@ -71,6 +72,7 @@ extern "C" void magma_queue_create_internal(magma_device_t device, magma_queue_t
 extern "C" void magma_queue_create_from_cuda_internal(magma_device_t device, void *cuda_stream,
                                                       void *, void *, magma_queue_t *queue_ptr,
                                                       const char *, const char *, int) {
+    mlu::tuning_load_env_once();
     magma_queue_t q = (magma_queue_t)calloc(1, sizeof(struct magma_queue));
     if (!q) { *queue_ptr = nullptr; return; }
     q->device = device;

@@ -137,6 +137,12 @@ _PROTOS["magma_dsposv_batched_work"] = ([c_int, c_int, c_int, c_ptr, c_int, c_pt
 _PROTOS["magma_dsposv_batched"] = ([c_int, c_int, c_int, c_ptr, c_int, c_ptr, c_int, c_ptr, c_int,
                                     c_ptr, c_ptr, c_int, c_ptr], c_int)
 _PROTOS["magma_lu_launch_count"] = ([], C.c_longlong)
+for _p in "ds":
+    _PROTOS[f"magma_{_p}getrf_batched_autotune"] = ([c_int, c_int, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}getrf_batched_tuning_get"] = ([c_ptr, c_ptr, c_ptr], c_int)
+    _PROTOS[f"magma_{_p}getrf_batched_tuning_set"] = ([c_ptr, c_ptr, c_ptr], c_int)
+_PROTOS["magma_lu_tuning_save"] = ([C.c_char_p], c_int)
+_PROTOS["magma_lu_tuning_load"] = ([C.c_char_p], c_int)
 _PROTOS["magma_lu_fail_allocations"] = ([c_int], c_int)
 _PROTOS["magma_sgetrf_batched_tc_wait_selftest"] = ([C.c_longlong, c_ptr, c_ptr], c_int)
 _PROTOS["magma_lu_timing_start"] = ([c_int, c_int], c_int)
