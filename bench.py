@@ -310,29 +310,40 @@ class Dsgesv512:
                 "peak_source": "FP32 FMA-throughput probe run inside bench.py "
                                "(magma_gb300/probe/peaks.cu)"}
 
-    # End to end: the batch goes through the C ABI as two calls, the first on a quarter
-    # of the matrices; all host-to-device copies are queued at once on a copy stream,
-    # so the second chunk arrives while the first is solved, and each chunk's solutions
-    # go back as soon as it is done.  (Measured on GB300: 13.6 ms per step with a
-    # quarter first, 14.1 ms with an eighth, 14.6 ms with a half, 15.5 ms as one call.)
-    E2E_CHUNKS = 2
-    E2E_FIRST = 0.25
+    # End to end: the batch goes through the C ABI as several calls on consecutive slices
+    # (E2E_SPLITS, fractions of the batch), issued round-robin on E2E_STREAMS queues (each
+    # with its own workspace); all host-to-device copies are queued at once on a copy
+    # stream, so later slices arrive while earlier ones are solved, and each slice's
+    # solutions go back as soon as it is done.  Measured on GB300 (ms per step of 512
+    # matrices): two halves on two queues 11.4; quarters on two queues 12.5; a quarter then
+    # three quarters on one queue 11.7-18.5 (the host's wake-up after each call's final
+    # read stays on the critical path with one queue, so it follows the host's load).
+    E2E_SPLITS = (0.5, 0.5)
+    E2E_STREAMS = 2
 
     def e2e_setup(self, c):
         import torch
-        from magma_gb300.batched import ptr_array
+        import magma_gb300 as mg
+        from magma_gb300.batched import ptr_array, Queue
         c["hS"] = c["S"].cpu().pin_memory()
         c["hB"] = c["B"].cpu().pin_memory()
         c["hX"] = torch.empty_like(c["hB"]).pin_memory()
         c["hIter"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
         c["hInfo"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
         c["copy_stream"] = torch.cuda.Stream()
-        first = int(self.batch * self.E2E_FIRST)
+        dev = c["S"].device
+        c["e2e_q"] = [(torch.cuda.current_stream(), c["q"], c["work"], c["lwork"])]
+        for _ in range(1, self.E2E_STREAMS):
+            st = torch.cuda.Stream()
+            w = torch.empty_like(c["work"])
+            c["e2e_q"].append((st, Queue(dev.index, st.cuda_stream), w, C.c_size_t(w.numel())))
+        bounds = np.round(np.cumsum((0.0,) + tuple(self.E2E_SPLITS)) * self.batch).astype(int)
         c["chunks"] = []
-        for k in range(self.E2E_CHUNKS):
-            sl = slice(0, first) if k == 0 else slice(first, self.batch)
+        for k in range(len(self.E2E_SPLITS)):
+            sl = slice(int(bounds[k]), int(bounds[k + 1]))
             c["chunks"].append({"sl": sl, "dS": ptr_array(c["Ss"][0][sl]), "dB": ptr_array(c["B"][sl]),
-                                "dX": ptr_array(c["X"][sl]), "dP": ptr_array(c["ipiv"][sl])})
+                                "dX": ptr_array(c["X"][sl]), "dP": ptr_array(c["ipiv"][sl]),
+                                "qi": k % self.E2E_STREAMS})
         h2d = c["hS"].numel() * 8 + c["hB"].numel() * 8
         d2h = c["hX"].numel() * 8 + 8 * self.batch
         return h2d, d2h
@@ -352,23 +363,41 @@ class Dsgesv512:
                 ev.record(cs)
                 arrived.append(ev)
         n, r = self.n, self.nrhs
-        for ck, ev in zip(c["chunks"], arrived):
-            sl = ck["sl"]
-            main.wait_event(ev)
-            rc = c["lib"].magma_dxgesv_gmres_batched_work(
-                PRECISIONS[self.precision], SOLVERS[self.solver], n, r, vp(ck["dS"]), n, vp(ck["dP"]),
-                vp(ck["dB"]), n, vp(ck["dX"]), n, vp(c["info"][sl]), vp(c["iter"][sl]),
-                self.itermax, self.tol, 1, vp(c["work"]), C.byref(c["lwork"]), sl.stop - sl.start,
-                c["q"].handle)
-            if rc != 0:
-                raise RuntimeError(f"magma_dxgesv_gmres_batched_work returned {rc}")
-            done = torch.cuda.Event()
-            done.record(main)
-            with torch.cuda.stream(cs):
-                cs.wait_event(done)
-                c["hX"][sl].copy_(c["X"][sl], non_blocking=True)
-                c["hIter"][sl].copy_(c["iter"][sl], non_blocking=True)
-                c["hInfo"][sl].copy_(c["info"][sl], non_blocking=True)
+
+        def run(qi):
+            # the calls of one queue, in order; a call returns once its slice is solved (it
+            # reads the count of matrices that need the FP64 re-solve), so several queues
+            # are driven from separate host threads
+            for ck, ev in zip(c["chunks"], arrived):
+                if ck["qi"] != qi:
+                    continue
+                sl = ck["sl"]
+                st, q, work, lwork = c["e2e_q"][qi]
+                st.wait_event(ev)
+                rc = c["lib"].magma_dxgesv_gmres_batched_work(
+                    PRECISIONS[self.precision], SOLVERS[self.solver], n, r, vp(ck["dS"]), n,
+                    vp(ck["dP"]), vp(ck["dB"]), n, vp(ck["dX"]), n, vp(c["info"][sl]),
+                    vp(c["iter"][sl]), self.itermax, self.tol, 1, vp(work), C.byref(lwork),
+                    sl.stop - sl.start, q.handle)
+                if rc != 0:
+                    raise RuntimeError(f"magma_dxgesv_gmres_batched_work returned {rc}")
+                done = torch.cuda.Event()
+                done.record(st)
+                with torch.cuda.stream(cs):
+                    cs.wait_event(done)
+                    c["hX"][sl].copy_(c["X"][sl], non_blocking=True)
+                    c["hIter"][sl].copy_(c["iter"][sl], non_blocking=True)
+                    c["hInfo"][sl].copy_(c["info"][sl], non_blocking=True)
+        if self.E2E_STREAMS == 1:
+            run(0)
+        else:
+            if "pool" not in c:
+                import concurrent.futures as cf
+                c["pool"] = cf.ThreadPoolExecutor(self.E2E_STREAMS)
+            for f in [c["pool"].submit(run, qi) for qi in range(self.E2E_STREAMS)]:
+                f.result()
+        for st, _, _, _ in c["e2e_q"]:
+            main.wait_stream(st)
         main.wait_stream(cs)                      # the step ends when the results are home
 
     def accuracy(self, c, last):
@@ -1462,7 +1491,8 @@ def run_ours(args, wl):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "calls_per_step": getattr(wl, "E2E_CHUNKS", 1),
+                "calls_per_step": len(getattr(wl, "E2E_SPLITS", (1,))),
+                "streams": getattr(wl, "E2E_STREAMS", 1),
                 "host_cpus": f"{len(cpus)} GPU-local cores" if cpus else "unpinned"},
         "gpu_launches": launches,
         "clocks": clk,

@@ -326,7 +326,7 @@ ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double
     }
     __syncthreads();
     if (SPD) chol_solve_smem<float, NR>(n, dAs_array[mat], ldas, sB);
-    else solve_smem<float, TRANS, NR>(n, dAs_array[mat], ldas, nullptr, sB, nr);
+    else solve_smem<float, TRANS, NR, true>(n, dAs_array[mat], ldas, nullptr, sB, nr);
     __syncthreads();
     double *X = dX_array[mat] + (size_t)c0 * lddx;
     for (int e = tid; e < nr * n; e += blockDim.x) {

@@ -295,8 +295,18 @@ __device__ __forceinline__ int panel_factor_regs(int pm, int ib, T *A, int lda, 
             } else {
                 const T l = nz ? rscale(a[r][0], piv, rcp) : a[r][0];
                 sP[(size_t)k * LDP + slot] = l;
+                // the row's remaining columns are j < ib - k: groups of eight past
+                // them are skipped (the same test in every lane of the block)
 #pragma unroll
-                for (int j = 1; j < PANEL_NB; j++) a[r][j - 1] = Prec<T>::fma_(-l, prow[j], a[r][j]);
+                for (int c = 0; c < PANEL_NB / 8; c++) {
+                    if (8 * c + 1 < ib - k) {
+#pragma unroll
+                        for (int jj = 0; jj < 8; jj++) {
+                            const int j = 8 * c + 1 + jj;
+                            if (j < PANEL_NB) a[r][j - 1] = Prec<T>::fma_(-l, prow[j], a[r][j]);
+                        }
+                    }
+                }
             }
         }
     }

@@ -42,11 +42,17 @@ __device__ __forceinline__ void stage_diag_block_async(const T *A, int ldda, int
     cp_async_commit();
 }
 
-template <typename T, bool TRANS, int SOLVE_NR>
+// PIPE (the refinement's correction solve): in the non-transposed solves the
+// next diagonal block is staged by cp.async while the current one is solved
+// (two buffers), and every thread loads its first row's 32 coefficients before
+// the diagonal solve.  Without PIPE the diagonal block is staged when it is
+// needed and the coefficients after it -- one buffer and fewer live registers,
+// for the kernels whose occupancy depends on them.
+template <typename T, bool TRANS, int SOLVE_NR, bool PIPE = false>
 __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, int nr)
 {
-    __shared__ T sD[32][33];
-    __shared__ T sDD[2][32][33];      // double-buffered diagonal blocks (no transpose)
+    __shared__ T sDD[(PIPE && !TRANS) ? 2 : 1][32][33];   // diagonal blocks
+    T (*sD)[33] = sDD[0];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (!TRANS) {
         if (ipiv != nullptr && tid < nr) {
@@ -61,29 +67,31 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
         // (staged one block ahead by cp.async) while every thread already has
         // the 32 coefficients of its first row below the block in flight; then
         // all threads update the rows below.
-        if (warp == 0) stage_diag_block_async<T>(A, ldda, 0, min(32, n), sDD[0]);
+        if (PIPE && warp == 0) stage_diag_block_async<T>(A, ldda, 0, min(32, n), sDD[0]);
         for (int t0 = 0, blk = 0; t0 < n; t0 += 32, blk++) {
             const int tb = min(32, n - t0);
             const int i0 = t0 + tb + tid;
             T lv[32];
-            if (tb == 32 && i0 < n) {
+            if (PIPE && tb == 32 && i0 < n) {
 #pragma unroll
                 for (int t = 0; t < 32; t++) lv[t] = A[i0 + (size_t)(t0 + t) * ldda];
             }
             if (warp == 0) {
-                if (t0 + 32 < n) {
+                if (!PIPE) {
+                    stage_diag_block<T>(A, ldda, t0, tb, sDD[0]);
+                } else if (t0 + 32 < n) {
                     stage_diag_block_async<T>(A, ldda, t0 + 32, min(32, n - t0 - 32), sDD[(blk + 1) & 1]);
                     cp_async_wait<1>();
                 } else {
                     cp_async_wait<0>();
                 }
                 __syncwarp();
-                T (*D)[33] = sDD[blk & 1];
+                T (*D)[33] = sDD[PIPE ? (blk & 1) : 0];
                 T y[SOLVE_NR];
                 const bool v = lane < tb;
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) y[c] = v ? sB[c * n + t0 + lane] : T(0);
-                if (tb == 32) {
+                if (PIPE && tb == 32) {
                     // unrolled: the coefficient loads run ahead of the shuffle chain
 #pragma unroll
                     for (int t = 0; t < 32; t++) {
@@ -113,8 +121,8 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
                 if (tb == 32) {
-                    // the row's 32 coefficients (the first row's are already here)
-                    if (i != i0) {
+                    // the row's 32 coefficients (with PIPE the first row's are already here)
+                    if (!PIPE || i != i0) {
 #pragma unroll
                         for (int t = 0; t < 32; t++) lv[t] = A[i + (size_t)(t0 + t) * ldda];
                     }
@@ -137,16 +145,19 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
             __syncthreads();
         }
         // backward: U x = y, the same overlap (blocks from the bottom)
-        if (warp == 0) stage_diag_block_async<T>(A, ldda, max(0, n - 32), n - max(0, n - 32), sDD[0]);
+        if (PIPE && warp == 0)
+            stage_diag_block_async<T>(A, ldda, max(0, n - 32), n - max(0, n - 32), sDD[0]);
         for (int t1 = n, blk = 0; t1 > 0; t1 -= 32, blk++) {
             const int t0 = max(0, t1 - 32), tb = t1 - t0;
             T uv0[32];
-            if (tb == 32 && tid < t0) {
+            if (PIPE && tb == 32 && tid < t0) {
 #pragma unroll
                 for (int t = 0; t < 32; t++) uv0[t] = A[tid + (size_t)(t0 + t) * ldda];
             }
             if (warp == 0) {
-                if (t0 > 0) {
+                if (!PIPE) {
+                    stage_diag_block<T>(A, ldda, t0, tb, sDD[0]);
+                } else if (t0 > 0) {
                     const int p0 = max(0, t0 - 32);
                     stage_diag_block_async<T>(A, ldda, p0, t0 - p0, sDD[(blk + 1) & 1]);
                     cp_async_wait<1>();
@@ -154,7 +165,7 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                     cp_async_wait<0>();
                 }
                 __syncwarp();
-                T (*sD)[33] = sDD[blk & 1];
+                T (*sD)[33] = sDD[PIPE ? (blk & 1) : 0];
                 T y[SOLVE_NR];
                 const bool v = lane < tb;
 #pragma unroll
@@ -162,7 +173,7 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 // lane t holds U(t0+t, t0+t) and its reciprocal, computed in parallel
                 const T dl = v ? sD[lane][lane] : T(1);
                 const T rl = T(1) / dl;
-                if (tb == 32) {
+                if (PIPE && tb == 32) {
                     // unrolled: coefficient loads and the diagonal shuffles run ahead
 #pragma unroll
                     for (int t = 31; t >= 0; t--) {
@@ -198,7 +209,7 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) acc[c] = sB[c * n + i];
                 if (tb == 32) {
-                    if (i != tid) {
+                    if (!PIPE || i != tid) {
 #pragma unroll
                         for (int t = 0; t < 32; t++) uv0[t] = A[i + (size_t)(t0 + t) * ldda];
                     }
