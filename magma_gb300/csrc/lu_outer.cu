@@ -77,19 +77,23 @@ __device__ __forceinline__ int ob_resolve(int x, int J, int K, const int *s_piv)
 
 // 64 updates of one k: rows la (4) and lb (4) of L against columns ua (4) and
 // ub (4) of U, acc[h][i][g][j] for row h*64 + tr*4 + i and column g*64 + tc*4 + j.
+// Column-major order (one U value against the eight L values) and a two-step
+// unroll of the k loop keep the kernel within 128 registers without spilling
+// (measured: 1.43 against 1.50 ms per factorisation with row-major order and
+// an eight-step unroll, which spilled).
 __device__ __forceinline__ void ob_fma(float (&acc)[2][4][2][4], const float4 &la, const float4 &lb,
                                        const float4 &ua, const float4 &ub)
 {
     const float l[2][4] = {{la.x, la.y, la.z, la.w}, {lb.x, lb.y, lb.z, lb.w}};
     const float u[2][4] = {{ua.x, ua.y, ua.z, ua.w}, {ub.x, ub.y, ub.z, ub.w}};
 #pragma unroll
-    for (int h = 0; h < 2; h++)
+    for (int g = 0; g < 2; g++)
 #pragma unroll
-        for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++)
 #pragma unroll
-            for (int g = 0; g < 2; g++)
+            for (int h = 0; h < 2; h++)
 #pragma unroll
-                for (int j = 0; j < 4; j++) acc[h][i][g][j] = fmaf(-l[h][i], u[g][j], acc[h][i][g][j]);
+                for (int i = 0; i < 4; i++) acc[h][i][g][j] = fmaf(-l[h][i], u[g][j], acc[h][i][g][j]);
 }
 
 // Triangular solve of the 32-row diagonal block kb for column c (one thread
@@ -369,7 +373,7 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
         const float *Lc = sL + (g % OB_RING) * OB_SSTAGE_FLOATS;
         const int kt = min(OB_SK, K - OB_SK * kc);
         if (kt == OB_SK) {
-#pragma unroll 8
+#pragma unroll 2
             for (int t = 0; t < OB_SK; t++) {
                 const int k = OB_SK * kc + t;
                 const float4 la = *reinterpret_cast<const float4 *>(Lc + t * OB_TM + tr * 4);
