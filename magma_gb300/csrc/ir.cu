@@ -89,6 +89,10 @@ extern "C" magma_int_t magma_dgesv_batched(magma_int_t n, magma_int_t nrhs, doub
 namespace mlu {
 
 constexpr int IR_ROWS = 128;       // rows per CTA in the FP64 kernels
+// rows per CTA of the residual: the later refinement passes have only the
+// unconverged matrices active, and 64-row CTAs spread them more evenly over
+// the SMs (residual class of the refinement benchmark 3.27 -> 3.11 ms per call)
+constexpr int IR_RES_ROWS = 64;
 constexpr int IR_NRHS_MAX = 16;
 constexpr int IR_SOLVE_NR = 8;
 constexpr int IR_ACTIVE = 0, IR_CONVERGED = 1, IR_FAILED = 2;
@@ -446,7 +450,7 @@ __global__ void ir_perm_kernel(IrShape sh, int **ipiv_array, int *perm)
 // or R = B - A^T X (a_ji in place of a_ij), with the column and row-sum
 // infinity norms of R and X.
 template <int NR, bool TRANS>
-__global__ void __launch_bounds__(IR_ROWS)
+__global__ void __launch_bounds__(IR_RES_ROWS)
 ir_residual_kernel(IrShape sh, double **dA_array, double **dB_array, double **dX_array, double *R,
                    unsigned long long *stats, int par)
 {
@@ -455,16 +459,16 @@ ir_residual_kernel(IrShape sh, double **dA_array, double **dB_array, double **dX
     const int mat = blockIdx.y, tid = threadIdx.x;
     const int n = sh.N(mat), nrhs = sh.NR(mat);
     const int ldda = sh.LDA(mat), lddb = sh.LDB(mat), lddx = sh.LDX(mat);
-    if (blockIdx.x * IR_ROWS >= n) return;            // whole CTA past this matrix
+    if (blockIdx.x * IR_RES_ROWS >= n) return;        // whole CTA past this matrix
     unsigned long long *st = stats + (size_t)mat * IR_STATS_WORDS;
     if (st[1] != IR_ACTIVE) return;
     const double *X = dX_array[mat];
-    for (int e = tid; e < n * NR; e += IR_ROWS) {
+    for (int e = tid; e < n * NR; e += IR_RES_ROWS) {
         const int j = e / NR, c = e % NR;
         sX[e] = c < nrhs ? X[j + (size_t)c * lddx] : 0.0;
     }
     __syncthreads();
-    const int i = blockIdx.x * IR_ROWS + tid;
+    const int i = blockIdx.x * IR_RES_ROWS + tid;
     double acc[NR];
     const double *A = dA_array[mat];
     const double *B = dB_array[mat];
@@ -942,7 +946,7 @@ static void launch_residual(const IrShape &sh, double **dA, double **dB, double 
     static size_t dyn_cache[MLU_MAX_DEVICES];
     mlu_device_cached(dyn_cache, [] { return mlu_allow_dynamic_smem(ir_residual_kernel<NR, TRANS>); });
     MLU_LAUNCH(mlu::KC_IR_RESIDUAL, s,
-               ir_residual_kernel<NR, TRANS><<<dim3((sh.n + IR_ROWS - 1) / IR_ROWS, batch), IR_ROWS,
+               ir_residual_kernel<NR, TRANS><<<dim3((sh.n + IR_RES_ROWS - 1) / IR_RES_ROWS, batch), IR_RES_ROWS,
                                                smem, s>>>(sh, dA, dB, dX, R, stats, par));
 }
 

@@ -180,12 +180,15 @@ small_gesv_packed_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_arr
 #pragma unroll 8
     for (int j = 0; j < 32; j++)
         sA[lane * PK_LD + j] = (live && row_valid && j < n) ? A[lane + (size_t)j * ldda] : T(0);
+    // one right-hand side lives in column 32 of sA (the row padding), so that its
+    // update rides in the packed update of each step
+    auto bref = [&](int row, int c) -> T & { return NRHS == 1 ? sA[row * PK_LD + 32] : sB[row * NB + c]; };
     T *B = nullptr;
     if (NRHS > 0) {
         B = live ? dB_array[mat] : nullptr;
 #pragma unroll
         for (int c = 0; c < NB; c++)
-            sB[lane * NB + c] = (live && row_valid && c < nrhs) ? B[lane + (size_t)c * lddb] : T(0);
+            bref(lane, c) = (live && row_valid && c < nrhs) ? B[lane + (size_t)c * lddb] : T(0);
     }
     __syncwarp();
     int info = 0, my_ipiv = 0;
@@ -210,9 +213,9 @@ small_gesv_packed_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_arr
                 sA[p * PK_LD + lane] = x;
             }
             if (NRHS > 0 && lane < NB) {
-                const T x = sB[k * NB + lane];
-                sB[k * NB + lane] = sB[p * NB + lane];
-                sB[p * NB + lane] = x;
+                const T x = bref(k, lane);
+                bref(k, lane) = bref(p, lane);
+                bref(p, lane) = x;
             }
         }
         if (lane == 0) s_piv[warp] = piv;
@@ -225,15 +228,18 @@ small_gesv_packed_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_arr
         __syncwarp();
         const int w = n - 1 - k;
         if (w > 0) {
-            const float inv = 1.0f / (float)w;
-            for (int e = lane; e < w * w; e += 32) {
+            // rows k+1.. by columns k+1..n-1, and column 32 (b) with one right-hand side
+            const int wc = NRHS == 1 ? w + 1 : w;
+            const float inv = 1.0f / (float)wc;
+            for (int e = lane; e < w * wc; e += 32) {
                 int i = __float2int_rz((float)e * inv);
-                int j = e - i * w;
-                if (j < 0) { i--; j += w; } else if (j >= w) { i++; j -= w; }
-                T *dst = sA + (k + 1 + i) * PK_LD + (k + 1 + j);
-                *dst = Prec<T>::fma_(-sA[(k + 1 + i) * PK_LD + k], sA[k * PK_LD + k + 1 + j], *dst);
+                int j = e - i * wc;
+                if (j < 0) { i--; j += wc; } else if (j >= wc) { i++; j -= wc; }
+                const int col = (NRHS == 1 && j == w) ? 32 : k + 1 + j;
+                T *dst = sA + (k + 1 + i) * PK_LD + col;
+                *dst = Prec<T>::fma_(-sA[(k + 1 + i) * PK_LD + k], sA[k * PK_LD + col], *dst);
             }
-            if (NRHS > 0 && lane > k && row_valid) {
+            if (NRHS > 1 && lane > k && row_valid) {
 #pragma unroll
                 for (int c = 0; c < NB; c++)
                     if (c < nrhs)
@@ -248,13 +254,13 @@ small_gesv_packed_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_arr
             const T d = sA[t * PK_LD + t], rr = sR[t];
             T x[NB];
 #pragma unroll
-            for (int c = 0; c < NB; c++) x[c] = rscale(sB[t * NB + c], d, rr);
+            for (int c = 0; c < NB; c++) x[c] = rscale(bref(t, c), d, rr);
             __syncwarp();
 #pragma unroll
             for (int c = 0; c < NB; c++) {
                 if (c < nrhs) {
-                    if (lane == t) sB[t * NB + c] = x[c];
-                    else if (lane < t) sB[lane * NB + c] = Prec<T>::fma_(-sA[lane * PK_LD + t], x[c], sB[lane * NB + c]);
+                    if (lane == t) bref(t, c) = x[c];
+                    else if (lane < t) bref(lane, c) = Prec<T>::fma_(-sA[lane * PK_LD + t], x[c], bref(lane, c));
                 }
             }
             __syncwarp();
@@ -268,7 +274,7 @@ small_gesv_packed_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_arr
         if (NRHS > 0) {
 #pragma unroll
             for (int c = 0; c < NB; c++)
-                if (c < nrhs) B[lane + (size_t)c * lddb] = sB[lane * NB + c];
+                if (c < nrhs) B[lane + (size_t)c * lddb] = bref(lane, c);
         }
     }
     if (live && lane == 0) info_array[mat] = info;
