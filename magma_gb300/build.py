@@ -18,6 +18,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libmagma_lu.so"
+BUILD_BC = PKG / "_build_bc"
+LIB_BC = PKG / "libmagma_lu_bc.so"
 PROBE_SRC = PKG / "probe" / "peaks.cu"
 PROBE_LIB = PKG / "libmlu_probe.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -45,8 +47,8 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _deps() + [PROBE_SRC])
 
 
-def _compile(src: Path, extra: list[str]) -> Path:
-    obj = BUILD / (src.stem + ".o")
+def _compile(src: Path, extra: list[str], outdir: Path = BUILD) -> Path:
+    obj = outdir / (src.stem + ".o")
     cmd = [nvcc_path(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-O2", "--expt-relaxed-constexpr", "-I", str(ROOT / "include"),
            *extra, "-c", str(src), "-o", str(obj)]
@@ -72,9 +74,26 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     return LIB
 
 
-def _link(objs: list[Path], out: Path) -> None:
+def build_bounds_check(force: bool = False) -> Path:
+    """The bounds-check build (-DMLU_BOUNDS_CHECK): the same sources with every
+    instrumented global access checked against its operand's logical extent, the
+    first violation recorded in a device word (mlu_bounds_check_read).  Separate
+    objects and library (libmagma_lu_bc.so); relocatable device code, so that
+    every translation unit records into the one word."""
+    if not force and LIB_BC.exists() and all(p.stat().st_mtime <= LIB_BC.stat().st_mtime for p in _deps()):
+        return LIB_BC
+    BUILD_BC.mkdir(exist_ok=True)
+    extra = ["-rdc=true", "-DMLU_BOUNDS_CHECK"]
+    srcs = sources()
+    with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, extra, BUILD_BC), srcs))
+    _link(objs, LIB_BC, ["-rdc=true"])
+    return LIB_BC
+
+
+def _link(objs: list[Path], out: Path, extra: list[str] | None = None) -> None:
     tmp = out.with_suffix(".so.tmp")
-    cmd = [nvcc_path(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc_path(), *ARCH, "-shared", *(extra or []), "-o", str(tmp), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -86,6 +86,23 @@ __device__ __forceinline__ unsigned warp_argmax_key(unsigned long long key, unsi
 template <typename T>
 __device__ __forceinline__ T shfl(T v, int src) { return __shfl_sync(FULL, v, src); }
 
+// ---------------------------------------------------------------------------
+// Bounds-check build (-DMLU_BOUNDS_CHECK, the library's stand-in for a memory
+// sanitizer): MLU_BC2(r, c, m, n, site) is true when element (r, c) lies inside
+// the logical m x n operand; otherwise it records the first violation (site,
+// r, c) in a device word, counts it, and is false, so that the caller skips the
+// access.  In the normal build it is the constant true and costs nothing.
+#ifdef MLU_BOUNDS_CHECK
+__device__ void bc_fail(int site, long long r, long long c);
+#define MLU_BC2(r, c, m, n, site)                                                         \
+    (((unsigned long long)(long long)(r) < (unsigned long long)(long long)(m) &&         \
+      (unsigned long long)(long long)(c) < (unsigned long long)(long long)(n))            \
+         ? true                                                                           \
+         : (mlu::bc_fail((site), (long long)(r), (long long)(c)), false))
+#else
+#define MLU_BC2(r, c, m, n, site) true
+#endif
+
 // cp.async of one element (4 or 8 bytes) to shared memory; `valid` false
 // writes zeros and reads nothing (src must still be a valid address).
 template <int BYTES>

@@ -439,7 +439,7 @@ __global__ void ir_perm_kernel(IrShape sh, int **ipiv_array, int *perm)
     if (threadIdx.x == 0) {
         for (int k = 0; k < n; k++) {
             const int p = ipiv[k] - 1;
-            if (p != k) { const int t = s_perm[k]; s_perm[k] = s_perm[p]; s_perm[p] = t; }
+            if (p != k && MLU_BC2(p, 0, n, 1, 501)) { const int t = s_perm[k]; s_perm[k] = s_perm[p]; s_perm[p] = t; }
         }
     }
     __syncthreads();

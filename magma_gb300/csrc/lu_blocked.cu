@@ -247,17 +247,18 @@ band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv
     // pivot targets, the band's original top rows and L11, all in flight together
     int p = j0 + lane;
     if (warp == 0 && ipiv_array != nullptr && lane < ib) p = ipiv_array[mat][j0 + lane] - 1;
+    if (warp == 0 && lane < ib && !MLU_BC2(p, 0, m, 1, 201)) p = j0 + lane;
     {
         float v[BAND_LOADS], l[PANEL_NB * PANEL_NB / BAND_THREADS];
 #pragma unroll
         for (int u = 0; u < BAND_LOADS; u++) {
             const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
-            v[u] = (k < ib && j < w) ? A[j0 + k + (size_t)(c0 + j) * ld] : 0.f;
+            v[u] = (k < ib && j < w && MLU_BC2(j0 + k, c0 + j, m, n, 202)) ? A[j0 + k + (size_t)(c0 + j) * ld] : 0.f;
         }
 #pragma unroll
         for (int u = 0; u < PANEL_NB * PANEL_NB / BAND_THREADS; u++) {
             const int e = tid + u * BAND_THREADS, i = e % PANEL_NB, t = e / PANEL_NB;
-            l[u] = (i < ib && t < ib) ? A[j0 + i + (size_t)(j0 + t) * ld] : 0.f;
+            l[u] = (i < ib && t < ib && MLU_BC2(j0 + i, j0 + t, m, n, 203)) ? A[j0 + i + (size_t)(j0 + t) * ld] : 0.f;
         }
         if (warp == 0) s_p[lane] = p;
 #pragma unroll
@@ -280,7 +281,8 @@ band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv
         for (int u = 0; u < BAND_LOADS; u++) {
             const int e = tid + u * BAND_THREADS, j = e % BAND_N, k = e / BAND_N;
             const int pk = s_p[k];
-            v[u] = (k < ib && pk >= r_first && j < w) ? A[pk + (size_t)(c0 + j) * ld] : 0.f;
+            v[u] = (k < ib && pk >= r_first && j < w && MLU_BC2(pk, c0 + j, m, n, 204))
+                       ? A[pk + (size_t)(c0 + j) * ld] : 0.f;
         }
         if (warp == 0) {
             // The step's interchanges k = 0..ib-1 exchange rows j0+k and p_k in
@@ -349,7 +351,8 @@ band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv
 #pragma unroll
     for (int u = 0; u < BAND_LOADS; u++) {
         const int e = tid + u * BAND_THREADS, k = e % PANEL_NB, j = e / PANEL_NB;
-        if (k < ib && j < w) A[j0 + k + (size_t)(c0 + j) * ld] = sU[k * BAND_U_LD + j];
+        if (k < ib && j < w && MLU_BC2(j0 + k, c0 + j, m, n, 205))
+            A[j0 + k + (size_t)(c0 + j) * ld] = sU[k * BAND_U_LD + j];
     }
     // strips of A22, one warp each
     for (int sidx = warp; sidx < nstrips; sidx += BAND_WARPS) {
@@ -362,8 +365,8 @@ band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv
         for (int c = 0; c < STRIP_N; c++) {
             const bool cv = cs + c < w;
             const float *colp = A + (size_t)(c0 + cs + c) * ld;
-            acc0[c] = (cv && ra < m) ? colp[ra] : 0.f;
-            acc1[c] = (cv && rb < m) ? colp[rb] : 0.f;
+            acc0[c] = (cv && ra < m && MLU_BC2(ra, c0 + cs + c, m, n, 206)) ? colp[ra] : 0.f;
+            acc1[c] = (cv && rb < m && MLU_BC2(rb, c0 + cs + c, m, n, 207)) ? colp[rb] : 0.f;
         }
         // rows of this strip that receive an original top row
         const int prow = s_row[lane];
@@ -406,8 +409,8 @@ band_kernel(int m, int n, int j0, int ib, float **dA_array, int ldda, int **ipiv
         for (int c = 0; c < STRIP_N; c++) {
             if (cs + c < w) {
                 float *colp = A + (size_t)(c0 + cs + c) * ld;
-                if (ra < m) colp[ra] = acc0[c];
-                if (rb < m) colp[rb] = acc1[c];
+                if (ra < m && MLU_BC2(ra, c0 + cs + c, m, n, 208)) colp[ra] = acc0[c];
+                if (rb < m && MLU_BC2(rb, c0 + cs + c, m, n, 209)) colp[rb] = acc1[c];
             }
         }
         __syncwarp();                                 // the buffer is refilled for the next strip
@@ -469,7 +472,10 @@ left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ip
     T *A = dA_array[mat];
     const int *ipiv = ipiv_array[mat];
     const int seg = m - ks, nk = ke - ks;
-    for (int k = tid; k < nk; k += LEFT_THREADS) s_piv[k] = ipiv[ks + k] - 1;
+    for (int k = tid; k < nk; k += LEFT_THREADS) {
+        s_piv[k] = ipiv[ks + k] - 1;
+        if (!MLU_BC2(s_piv[k], 0, m, 1, 301)) s_piv[k] = ks + k;
+    }
     __syncthreads();
     int tau[LEFT_ROWS];
 #pragma unroll
@@ -488,7 +494,8 @@ left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ip
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const int e = e0 + u * LEFT_THREADS;
-                if (e < total) v[u] = A[ks + e % seg + (size_t)(cb + e / seg) * ldda];
+                if (e < total && MLU_BC2(ks + e % seg, cb + e / seg, m, n, 302))
+                    v[u] = A[ks + e % seg + (size_t)(cb + e / seg) * ldda];
             }
 #pragma unroll
             for (int u = 0; u < 8; u++) {
@@ -501,7 +508,7 @@ left_swaps_kernel(int m, int n, int gm, int gn, T **dA_array, int ldda, int **ip
 #pragma unroll
             for (int u = 0; u < LEFT_ROWS; u++) {
                 const int i = ks + tid + u * LEFT_THREADS, src = tau[u] - ks;
-                if (i < m && tau[u] != i && src >= 0 && src < seg)
+                if (i < m && tau[u] != i && src >= 0 && src < seg && MLU_BC2(i, cb + c, m, n, 303))
                     A[i + (size_t)(cb + c) * ldda] = sbuf[c * seg + src];
             }
         }

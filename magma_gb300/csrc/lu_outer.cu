@@ -197,6 +197,7 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
     //    interchange touches always ends up holding an original top row.
     if (tid < OUTER_NB)
         s_piv[tid] = tid < K ? (ipiv_array ? ipiv_array[mat][J + tid] - 1 : J + tid) : 0;
+    if (tid < K && !MLU_BC2(s_piv[tid], 0, m, 1, 101)) s_piv[tid] = J + tid;
     if (tid < OB_MAX_ROWS / 32) s_dmask[tid] = 0u;
     if (tid == 0) s_nt = 0;
     __syncthreads();
@@ -224,7 +225,8 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
         for (int u = 0; u < 32; u++) {
             const int idx = tid + (u0 + u) * OB_THREADS;
             const int k = ((idx >> 5) & 15) * 8 + (idx & 7), c = (idx >> 9) * 4 + ((idx >> 3) & 3);
-            v[u] = (k < K && c < w) ? A[s_top[k] + (size_t)(c0 + c) * ld] : 0.f;
+            v[u] = (k < K && c < w && MLU_BC2(s_top[k], c0 + c, m, n, 102)) ? A[s_top[k] + (size_t)(c0 + c) * ld]
+                                                                           : 0.f;
         }
 #pragma unroll
         for (int u = 0; u < 32; u++) {
@@ -338,7 +340,7 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
                     for (int j = 0; j < 4; j++) {
                         const int col = gg * 64 + tc * 4 + j;
                         const float *colp = A + (size_t)(c0 + col) * ld;
-                        if (v4 && col < w) {
+                        if (v4 && col < w && MLU_BC2(r0 + rb + 3, c0 + col, m, n, 103)) {
                             const float4 x = *reinterpret_cast<const float4 *>(colp + r0 + rb);
                             acc[h][0][gg][j] = x.x;
                             acc[h][1][gg][j] = x.y;
@@ -347,7 +349,9 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
                         } else {
 #pragma unroll
                             for (int i = 0; i < 4; i++)
-                                acc[h][i][gg][j] = (r0 + rb + i < m && col < w) ? colp[r0 + rb + i] : 0.f;
+                                acc[h][i][gg][j] =
+                                    (r0 + rb + i < m && col < w && MLU_BC2(r0 + rb + i, c0 + col, m, n, 104))
+                                        ? colp[r0 + rb + i] : 0.f;
                         }
                     }
                 if (dm) {
@@ -360,7 +364,8 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
 #pragma unroll
                                 for (int j = 0; j < 4; j++) {
                                     const int col = gg * 64 + tc * 4 + j;
-                                    if (col < w) acc[h][i][gg][j] = A[src + (size_t)(c0 + col) * ld];
+                                    if (col < w && MLU_BC2(src, c0 + col, m, n, 105))
+                                        acc[h][i][gg][j] = A[src + (size_t)(c0 + col) * ld];
                                 }
                         }
                     }
@@ -406,13 +411,14 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
                         const int col = gg * 64 + tc * 4 + j;
                         if (col >= w) continue;
                         float *colp = A + (size_t)(c0 + col) * ld + r0 + rb;
-                        if (v4) {
+                        if (v4 && MLU_BC2(r0 + rb + 3, c0 + col, m, n, 106)) {
                             *reinterpret_cast<float4 *>(colp) =
                                 make_float4(acc[h][0][gg][j], acc[h][1][gg][j], acc[h][2][gg][j], acc[h][3][gg][j]);
                         } else {
 #pragma unroll
                             for (int i = 0; i < 4; i++)
-                                if (r0 + rb + i < m) colp[i] = acc[h][i][gg][j];
+                                if (r0 + rb + i < m && MLU_BC2(r0 + rb + i, c0 + col, m, n, 107))
+                                    colp[i] = acc[h][i][gg][j];
                         }
                     }
             }
@@ -427,7 +433,8 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
         for (int x = tid; x < nt * w; x += OB_THREADS) {
             const int e = x % nt, c = x / nt;
             float *colp = A + (size_t)(c0 + c) * ld;
-            colp[E + s_drow[e]] = colp[s_dsrc[e]];
+            if (MLU_BC2(E + s_drow[e], c0 + c, m, n, 108) && MLU_BC2(s_dsrc[e], c0 + c, m, n, 109))
+                colp[E + s_drow[e]] = colp[s_dsrc[e]];
         }
         H *U = Ub + (size_t)mat * upad * OUTER_NB + (size_t)(c0 - E) * OUTER_NB;
 #pragma unroll 4
@@ -443,7 +450,7 @@ outer_update_kernel(int m, int n, int J, float **dA_array, int ldda, int **ipiv_
     for (int u = 0; u < OB_U_FLOATS / OB_THREADS; u++) {
         const int idx = tid + u * OB_THREADS;
         const int k = ((idx >> 5) & 15) * 8 + (idx & 7), c = (idx >> 9) * 4 + ((idx >> 3) & 3);
-        if (k < K && c < w) A[J + k + (size_t)(c0 + c) * ld] = sU[ob_uidx(k, c)];
+        if (k < K && c < w && MLU_BC2(J + k, c0 + c, m, n, 110)) A[J + k + (size_t)(c0 + c) * ld] = sU[ob_uidx(k, c)];
     }
 }
 

@@ -206,7 +206,7 @@ small_gesv_packed_kernel(int n, int nrhs, T **dA_array, int ldda, int **ipiv_arr
         const bool nz = Prec<T>::nonzero(piv);
         if (!nz && info == 0) info = k + 1;
         if (lane == k) my_ipiv = p + 1;
-        if (p != k) {                                   // whole rows k and p, and the right-hand sides
+        if (p != k && MLU_BC2(p, 0, n, 1, 601)) {       // whole rows k and p, and the right-hand sides
             if (row_valid) {
                 const T x = sA[k * PK_LD + lane];
                 sA[k * PK_LD + lane] = sA[p * PK_LD + lane];

@@ -184,3 +184,37 @@ extern "C" void magma_iset_pointer(magma_int_t **output_array, magma_int_t *inpu
                                    magma_queue_t queue) {
     set_pointer(output_array, input, lda, row, column, batch_offset, batchCount, queue);
 }
+
+#ifdef MLU_BOUNDS_CHECK
+// The bounds-check build's record: the first violation (site << 48 | row << 24
+// | column, each clipped to 24 bits) and the number of violations.
+namespace mlu {
+__device__ unsigned long long g_bc_first;
+__device__ unsigned long long g_bc_count;
+__device__ void bc_fail(int site, long long r, long long c)
+{
+    const unsigned long long rec = ((unsigned long long)(site & 0xffff) << 48) |
+                                   (((unsigned long long)r & 0xffffffull) << 24) |
+                                   ((unsigned long long)c & 0xffffffull);
+    atomicCAS(&g_bc_first, 0ull, rec);
+    atomicAdd(&g_bc_count, 1ull);
+}
+}  // namespace mlu
+
+// Reads the record (first violation, count) and, with reset != 0, clears it.
+// Exported by the bounds-check build only.
+extern "C" int mlu_bounds_check_read(unsigned long long *first, unsigned long long *count, int reset)
+{
+    if (cudaDeviceSynchronize() != cudaSuccess) return -1;
+    if (cudaMemcpyFromSymbol(first, mlu::g_bc_first, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemcpyFromSymbol(count, mlu::g_bc_count, sizeof(unsigned long long)) != cudaSuccess)
+        return -1;
+    if (reset) {
+        const unsigned long long z = 0;
+        if (cudaMemcpyToSymbol(mlu::g_bc_first, &z, sizeof z) != cudaSuccess ||
+            cudaMemcpyToSymbol(mlu::g_bc_count, &z, sizeof z) != cudaSuccess)
+            return -1;
+    }
+    return 0;
+}
+#endif

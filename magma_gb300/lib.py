@@ -177,6 +177,32 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
         return lib
 
 
+_lib_bc = None
+
+
+def load_bounds_checked() -> C.CDLL:
+    """The bounds-check build of the library (libmagma_lu_bc.so, built on first use
+    with -DMLU_BOUNDS_CHECK): the same entry points, plus
+    mlu_bounds_check_read(&first, &count, reset), the record of global accesses
+    that fell outside their operand.  Test infrastructure; it loads beside the
+    normal library without sharing state with it."""
+    global _lib_bc
+    with _lock:
+        if _lib_bc is not None:
+            return _lib_bc
+        from . import build as _build
+        p = _build.build_bounds_check()
+        lib = C.CDLL(str(p))
+        for name, (args, res) in _PROTOS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        lib.mlu_bounds_check_read.argtypes = [C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong), C.c_int]
+        lib.mlu_bounds_check_read.restype = C.c_int
+        _lib_bc = lib
+        return lib
+
+
 def exported_names() -> list[str]:
     return sorted(_PROTOS)
 
