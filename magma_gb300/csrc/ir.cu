@@ -273,8 +273,8 @@ __device__ __forceinline__ bool ir_converged(const unsigned long long *st, int p
 // whole batch of 512 matrices resident at once beats more registers per thread.
 // SPD: the factors are the FP32 Cholesky factor L (lower), the correction is
 // L L^T d = r (no interchanges, no scaling).
-template <int NR, bool TRANS, bool SPD = false>
-__global__ void __launch_bounds__(256, 4)
+template <int NR, bool TRANS, bool SPD = false, int NT = 256>
+__global__ void __launch_bounds__(NT, NT == 256 ? 4 : 2)
 ir_solve_kernel(IrShape sh, float **dAs_array, int ldas, const int *perm, double **dX_array,
                 const double *R, unsigned long long *stats, int *iter, const int *info, int it,
                 double tol, const double *rowscale, const double *colscale)
@@ -961,6 +961,18 @@ static void residual(const IrShape &sh, double **dA, double **dB, double **dX, d
     else                   launch_residual<16, TRANS>(sh, dA, dB, dX, R, stats, par, batch, s);
 }
 
+// SMs of the current device (cached per device).
+static int ir_sm_count()
+{
+    static size_t cache[MLU_MAX_DEVICES];
+    return (int)mlu_device_cached(cache, [] {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        return (size_t)sms;
+    });
+}
+
 // check + correction solve of refinement iteration `it` (-1: the initial solve)
 template <bool TRANS>
 static void correction_solve(const IrShape &sh, float **As_array, int ldas, const int *perm,
@@ -978,6 +990,18 @@ static void correction_solve(const IrShape &sh, float **As_array, int ldas, cons
         else
             MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<IR_SOLVE_NR, false, true><<<grid, 256, ssmem, s>>>(
                 sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, nullptr, nullptr));
+        return;
+    }
+    // a batch that two CTAs per SM hold at once gets 512-thread CTAs: each matrix's
+    // updates below its diagonal blocks spread over twice the threads (the largest
+    // matrix's chain of blocks is the launch's critical path)
+    if ((size_t)grid.x * grid.y <= 2 * (size_t)ir_sm_count()) {
+        if (snr == 4)
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<4, TRANS, false, 512><<<grid, 512, ssmem, s>>>(
+                sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, rsc, csc));
+        else
+            MLU_LAUNCH(mlu::KC_IR_SOLVE, s, ir_solve_kernel<IR_SOLVE_NR, TRANS, false, 512><<<grid, 512, ssmem, s>>>(
+                sh, As_array, ldas, perm, dX, R, stats, iter, info, it, tol, rsc, csc));
         return;
     }
     if (snr == 4)
@@ -1028,8 +1052,12 @@ static size_t solve_dyn_max()
                            mlu_allow_dynamic_smem(ir_solve_kernel<4, false>)),
                        min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, true>),
                            mlu_allow_dynamic_smem(ir_solve_kernel<4, true>))),
-                   min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false, true>),
-                       mlu_allow_dynamic_smem(ir_solve_kernel<4, false, true>)));
+                   min(min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false, true>),
+                           mlu_allow_dynamic_smem(ir_solve_kernel<4, false, true>)),
+                       min(min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, false, false, 512>),
+                               mlu_allow_dynamic_smem(ir_solve_kernel<4, false, false, 512>)),
+                           min(mlu_allow_dynamic_smem(ir_solve_kernel<IR_SOLVE_NR, true, false, 512>),
+                               mlu_allow_dynamic_smem(ir_solve_kernel<4, true, false, 512>)))));
     });
 }
 

@@ -48,10 +48,30 @@ __device__ __forceinline__ void stage_diag_block_async(const T *A, int ldda, int
 // the diagonal solve.  Without PIPE the diagonal block is staged when it is
 // needed and the coefficients after it -- one buffer and fewer live registers,
 // for the kernels whose occupancy depends on them.
+// NR consecutive values from shared memory, 16 bytes at a time (FP32, NR a
+// multiple of 4).  The loads are volatile so that the compiler re-reads them per
+// row instead of keeping every row's worth in registers.
+template <typename T, int NR>
+__device__ __forceinline__ void load_row_smem(const T *p, T (&v)[NR])
+{
+    static_assert(sizeof(T) == 4 && NR % 4 == 0, "FP32 rows of a multiple of four");
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+#pragma unroll
+    for (int q = 0; q < NR / 4; q++)
+        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];\n"
+                     : "=f"(v[4 * q]), "=f"(v[4 * q + 1]), "=f"(v[4 * q + 2]), "=f"(v[4 * q + 3])
+                     : "r"(a + 16 * q)
+                     : "memory");
+}
+
 template <typename T, bool TRANS, int SOLVE_NR, bool PIPE = false>
 __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, int nr)
 {
     __shared__ T sDD[(PIPE && !TRANS) ? 2 : 1][32][33];   // diagonal blocks
+    // (PIPE) the diagonal block's solution, right-hand sides contiguous, so that the
+    // update below reads all of one row's values in one or two 16-byte loads
+    constexpr int YR = (PIPE && !TRANS) ? 32 : 1, YC = (PIPE && !TRANS) ? SOLVE_NR : 1;
+    __shared__ __align__(16) T sY[YR][YC];
     T (*sD)[33] = sDD[0];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (!TRANS) {
@@ -114,6 +134,10 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 }
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) if (v) sB[c * n + t0 + lane] = y[c];
+                if (PIPE && v) {
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++) sY[lane % YR][c % YC] = y[c];
+                }
             }
             __syncthreads();
             for (int i = i0; i < n; i += blockDim.x) {
@@ -127,10 +151,13 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                         for (int t = 0; t < 32; t++) lv[t] = A[i + (size_t)(t0 + t) * ldda];
                     }
 #pragma unroll
-                    for (int t = 0; t < 32; t++)
+                    for (int t = 0; t < 32; t++) {
+                        T yv[SOLVE_NR];
+                        if constexpr (PIPE) load_row_smem<T, SOLVE_NR>(&sY[t % YR][0], yv);
 #pragma unroll
                         for (int c = 0; c < SOLVE_NR; c++)
-                            acc[c] = Prec<T>::fma_(-lv[t], sB[c * n + t0 + t], acc[c]);
+                            acc[c] = Prec<T>::fma_(-lv[t], PIPE ? yv[c] : sB[c * n + t0 + t], acc[c]);
+                    }
                 } else {
                     for (int t = 0; t < tb; t++) {
                         const T l = A[i + (size_t)(t0 + t) * ldda];
@@ -202,6 +229,10 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                 }
 #pragma unroll
                 for (int c = 0; c < SOLVE_NR; c++) if (v) sB[c * n + t0 + lane] = y[c];
+                if (PIPE && v) {
+#pragma unroll
+                    for (int c = 0; c < SOLVE_NR; c++) sY[lane % YR][c % YC] = y[c];
+                }
             }
             __syncthreads();
             for (int i = tid; i < t0; i += blockDim.x) {
@@ -214,10 +245,13 @@ __device__ void solve_smem(int n, const T *A, int ldda, const int *ipiv, T *sB, 
                         for (int t = 0; t < 32; t++) uv0[t] = A[i + (size_t)(t0 + t) * ldda];
                     }
 #pragma unroll
-                    for (int t = 31; t >= 0; t--)
+                    for (int t = 31; t >= 0; t--) {
+                        T yv[SOLVE_NR];
+                        if constexpr (PIPE) load_row_smem<T, SOLVE_NR>(&sY[t % YR][0], yv);
 #pragma unroll
                         for (int c = 0; c < SOLVE_NR; c++)
-                            acc[c] = Prec<T>::fma_(-uv0[t], sB[c * n + t0 + t], acc[c]);
+                            acc[c] = Prec<T>::fma_(-uv0[t], PIPE ? yv[c] : sB[c * n + t0 + t], acc[c]);
+                    }
                 } else {
                     for (int t = tb - 1; t >= 0; t--) {
                         const T u = A[i + (size_t)(t0 + t) * ldda];
