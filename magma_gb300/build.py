@@ -79,15 +79,19 @@ def build_bounds_check(force: bool = False) -> Path:
     instrumented global access checked against its operand's logical extent, the
     first violation recorded in a device word (mlu_bounds_check_read).  Separate
     objects and library (libmagma_lu_bc.so); relocatable device code, so that
-    every translation unit records into the one word."""
+    every translation unit records into the one word.  Its function-local statics (the
+    per-device caches of kernel attributes) are ordinary weak symbols bound inside the
+    library (-fno-gnu-unique, -Bsymbolic): as GNU-unique symbols the dynamic linker would
+    merge them with the normal library's in a process that loads both, and one library's
+    filled cache would keep the other from setting its kernels' attributes."""
     if not force and LIB_BC.exists() and all(p.stat().st_mtime <= LIB_BC.stat().st_mtime for p in _deps()):
         return LIB_BC
     BUILD_BC.mkdir(exist_ok=True)
-    extra = ["-rdc=true", "-DMLU_BOUNDS_CHECK"]
+    extra = ["-rdc=true", "-DMLU_BOUNDS_CHECK", "-Xcompiler", "-fno-gnu-unique"]
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra, BUILD_BC), srcs))
-    _link(objs, LIB_BC, ["-rdc=true"])
+    _link(objs, LIB_BC, ["-rdc=true", "-Xlinker", "-Bsymbolic"])
     return LIB_BC
 
 
