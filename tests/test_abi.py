@@ -138,3 +138,32 @@ def test_header_is_c99_and_links(lib, tmp_path):
                           str(src), f"-L{libdir}", "-lmagma_lu", f"-Wl,-rpath,{libdir}", "-o",
                           str(tmp_path / "caller")], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
+
+
+def _dynamic_symbol_bindings(path):
+    """(binding, name) of every dynamic symbol of a shared library, from readelf."""
+    import shutil
+    import subprocess
+    if shutil.which("readelf") is None:
+        pytest.skip("readelf is not installed")
+    out = subprocess.run(["readelf", "-W", "--dyn-syms", str(path)], capture_output=True, text=True).stdout
+    rows = []
+    for line in out.splitlines():
+        f = line.split()
+        if len(f) >= 8 and f[0].rstrip(":").isdigit():
+            rows.append((f[4], f[7]))
+    return rows
+
+
+def test_bounds_check_build_exports_and_binds_locally():
+    """The bounds-check library (tests/test_gpu_bounds_check.py loads it beside the normal
+    one) exports every declared entry point and its record reader, and holds no GNU-unique
+    symbols: those the dynamic linker would merge with the normal library's, sharing its
+    per-device kernel-attribute caches across the two libraries."""
+    from magma_gb300 import build as B
+    path = B.build_bounds_check()
+    bc = C.CDLL(str(path))
+    missing = [n for n in declared_functions() + ["mlu_bounds_check_read"] if not hasattr(bc, n)]
+    assert not missing, missing
+    unique = [name for binding, name in _dynamic_symbol_bindings(path) if binding == "UNIQUE"]
+    assert not unique, unique[:5]
