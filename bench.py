@@ -129,22 +129,57 @@ class Gesv32:
     dominant_class = "small_gesv"
     dominant = "mlu::small_gesv_kernel<double,32,1>"
 
+    # End to end: two calls on the two halves of the batch; the second half's host-to-device
+    # copy runs on a copy stream while the first half is solved, and each half's solutions
+    # go back as soon as it is done.  (Measured on GB300: 0.77 ms per step, 0.84 as one call.)
+    E2E_HALVES = 2
+
     def e2e_setup(self, c):
         import torch
+        from magma_gb300.batched import ptr_array
         c["hS"] = torch.from_numpy(c["S_h"]).pin_memory()
         c["hB"] = torch.from_numpy(c["B_h"]).pin_memory()
         c["hX"] = torch.empty_like(c["hB"]).pin_memory()
         c["hInfo"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
+        c["copy_stream"] = torch.cuda.Stream()
+        bounds = np.linspace(0, self.batch, self.E2E_HALVES + 1).astype(int)
+        c["halves"] = []
+        for k in range(self.E2E_HALVES):
+            sl = slice(int(bounds[k]), int(bounds[k + 1]))
+            c["halves"].append({"sl": sl, "dA": ptr_array(c["S"][0][sl]), "dX": ptr_array(c["X"][0][sl]),
+                                "dP": ptr_array(c["ipiv"][sl])})
         h2d = c["hS"].numel() * 8 + c["hB"].numel() * 8
         d2h = c["hX"].numel() * 8 + c["hInfo"].numel() * 4
         return h2d, d2h
 
     def e2e_step(self, c):
-        c["S"][0].copy_(c["hS"], non_blocking=True)
-        c["X"][0].copy_(c["hB"], non_blocking=True)
-        self.step(c, 0)
-        c["hX"].copy_(c["X"][0], non_blocking=True)
-        c["hInfo"].copy_(c["info"], non_blocking=True)
+        import torch
+        main, cs = torch.cuda.current_stream(), c["copy_stream"]
+        cs.wait_stream(main)                      # the previous step is done with the buffers
+        arrived = []
+        with torch.cuda.stream(cs):
+            for hf in c["halves"]:
+                sl = hf["sl"]
+                c["S"][0][sl].copy_(c["hS"][sl], non_blocking=True)
+                c["X"][0][sl].copy_(c["hB"][sl], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                arrived.append(ev)
+        for hf, ev in zip(c["halves"], arrived):
+            sl = hf["sl"]
+            main.wait_event(ev)
+            rc = c["lib"].magma_dgesv_batched(self.n, self.nrhs, vp(hf["dA"]), self.n, vp(hf["dP"]),
+                                              vp(hf["dX"]), self.n, vp(c["info"][sl]), sl.stop - sl.start,
+                                              c["q"].handle)
+            if rc != 0:
+                raise RuntimeError(f"magma_dgesv_batched returned {rc}")
+            done = torch.cuda.Event()
+            done.record(main)
+            with torch.cuda.stream(cs):
+                cs.wait_event(done)
+                c["hX"][sl].copy_(c["X"][0][sl], non_blocking=True)
+                c["hInfo"][sl].copy_(c["info"][sl], non_blocking=True)
+        main.wait_stream(cs)                      # the step ends when the results are home
 
     def accuracy(self, c, last):
         n = self.n
@@ -1491,7 +1526,8 @@ def run_ours(args, wl):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "solves/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
-                "calls_per_step": len(getattr(wl, "E2E_SPLITS", (1,))),
+                "calls_per_step": (len(wl.E2E_SPLITS) if hasattr(wl, "E2E_SPLITS")
+                                   else getattr(wl, "E2E_HALVES", 1)),
                 "streams": getattr(wl, "E2E_STREAMS", 1),
                 "host_cpus": f"{len(cpus)} GPU-local cores" if cpus else "unpinned"},
         "gpu_launches": launches,
