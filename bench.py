@@ -741,20 +741,47 @@ class Adjoint2048:
         c["dA"] = torch.empty_like(c["A0"])
         c["dB"] = torch.empty_like(c["B0"])
         c["dg"] = torch.empty_like(c["gX"])
+        c["copy_stream"] = torch.cuda.Stream()
         h2d = (c["hA"].numel() + c["hB"].numel() + c["hgX"].numel()) * 8
         d2h = (c["hgA"].numel() + c["hgB"].numel()) * 8
         return h2d, d2h
 
+    # End to end: the batch as two halves, each its own forward + backward; the second half's
+    # inputs arrive on a copy stream while the first is solved, and each half's gradients go
+    # back as soon as they are computed.  (Measured on GB300: 1.88 ms per step, 1.96 as one pass.)
+    E2E_HALVES = 2
+
     def e2e_step(self, c):
+        import torch
         from magma_gb300.autograd import solve
-        c["dA"].copy_(c["hA"], non_blocking=True)
-        c["dB"].copy_(c["hB"], non_blocking=True)
-        c["dg"].copy_(c["hgX"], non_blocking=True)
-        A = c["dA"].detach().requires_grad_(True)
-        B = c["dB"].detach().requires_grad_(True)
-        solve(A, B).backward(c["dg"])
-        c["hgA"].copy_(A.grad, non_blocking=True)
-        c["hgB"].copy_(B.grad, non_blocking=True)
+        main, cs = torch.cuda.current_stream(), c["copy_stream"]
+        cs.wait_stream(main)                      # the previous step is done with the buffers
+        bounds = np.linspace(0, self.batch, self.E2E_HALVES + 1).astype(int)
+        halves = [slice(int(bounds[k]), int(bounds[k + 1])) for k in range(self.E2E_HALVES)]
+        arrived = []
+        with torch.cuda.stream(cs):
+            for sl in halves:
+                c["dA"][sl].copy_(c["hA"][sl], non_blocking=True)
+                c["dB"][sl].copy_(c["hB"][sl], non_blocking=True)
+                c["dg"][sl].copy_(c["hgX"][sl], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                arrived.append(ev)
+        for sl, ev in zip(halves, arrived):
+            main.wait_event(ev)
+            A = c["dA"][sl].detach().requires_grad_(True)
+            B = c["dB"][sl].detach().requires_grad_(True)
+            solve(A, B).backward(c["dg"][sl])
+            done = torch.cuda.Event()
+            done.record(main)
+            gA, gB = A.grad, B.grad
+            with torch.cuda.stream(cs):
+                cs.wait_event(done)
+                c["hgA"][sl].copy_(gA, non_blocking=True)
+                c["hgB"][sl].copy_(gB, non_blocking=True)
+                gA.record_stream(cs)
+                gB.record_stream(cs)
+        main.wait_stream(cs)                      # the step ends when the gradients are home
 
     def accuracy(self, c, last):
         import torch
