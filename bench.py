@@ -624,7 +624,8 @@ class GesvVbatched:
     def _call(self, c, A, B, q):
         rc = c["lib"].magma_dgesv_vbatched_max_nocheck_work(
             vp(A.ncols), vp(B.ncols), 256, 16, vp(A.ptrs), vp(A.ld), vp(c["dP"]), vp(B.ptrs),
-            vp(B.ld), vp(c["info"]), vp(c["work"]), C.byref(c["lwork"]), self.batch, q.handle)
+            vp(B.ld), vp(c["info"]), vp(c["work"]), C.byref(c["lwork"]), c.get("b", self.batch),
+            q.handle)
         if rc != 0:
             raise RuntimeError(f"magma_dgesv_vbatched_max_nocheck_work returned {rc}")
 
@@ -638,20 +639,80 @@ class GesvVbatched:
     graph_kernels_per_step = 2
     dominant = "mlu::vb_lu_kernel<double> (persistent)"
 
+    # End to end: the batch as two halves, each with its own buffers and captured graph; the
+    # second half's inputs arrive on a copy stream while the first half's graph runs, and each
+    # half's solutions go back as soon as its graph is done.  (Measured on GB300: 26.2 ms per
+    # step, 31.7 as one graph.)
+    E2E_HALVES = 2
+
+    def _half(self, dev, lib, ns, As, Bs):
+        """Buffers, workspace and a captured graph for the matrices given."""
+        import torch
+        from magma_gb300.batched import VBatch, Queue
+        b = len(ns)
+        hc = {"lib": lib, "b": b}
+        hc["A"] = VBatch([a.shape for a in As], ns, torch.float64, dev).load(As)
+        hc["B"] = VBatch([x.shape for x in Bs], ns, torch.float64, dev).load(Bs)
+        offs = np.concatenate([[0], np.cumsum(ns)[:-1]])
+        hc["ipiv"] = torch.zeros((sum(ns),), dtype=torch.int32, device=dev)
+        hc["dP"] = hc["ipiv"].data_ptr() + torch.tensor(offs, dtype=torch.int64, device=dev) * 4
+        hc["info"] = torch.empty((b,), dtype=torch.int32, device=dev)
+        lw = C.c_int(-1)
+        lib.magma_dgesv_vbatched_max_nocheck_work(None, None, 256, 16, None, None, None, None,
+                                                  None, None, None, C.byref(lw), b, None)
+        hc["lwork"] = lw
+        hc["work"] = torch.empty((lw.value,), dtype=torch.uint8, device=dev)
+        stream = torch.cuda.Stream(dev)
+        hc["gq"] = Queue(dev.index, stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        with torch.cuda.stream(stream):
+            self._call(hc, hc["A"], hc["B"], hc["gq"])   # eager once (kernel attributes)
+            stream.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                self._call(hc, hc["A"], hc["B"], hc["gq"])
+        hc["graph"] = g
+        hc["hA"] = hc["A"].buf.cpu().pin_memory()
+        hc["hB"] = hc["B"].buf.cpu().pin_memory()
+        hc["hX"] = torch.empty_like(hc["hB"]).pin_memory()
+        hc["hInfo"] = torch.empty((b,), dtype=torch.int32).pin_memory()
+        torch.cuda.synchronize(dev)
+        return hc
+
     def e2e_setup(self, c):
         import torch
-        c["hA"] = c["A0"].buf.cpu().pin_memory()
-        c["hB"] = c["B0"].buf.cpu().pin_memory()
-        c["hX"] = torch.empty_like(c["hB"]).pin_memory()
-        c["hInfo"] = torch.empty((self.batch,), dtype=torch.int32).pin_memory()
-        return c["hA"].numel() * 8 + c["hB"].numel() * 8, c["hX"].numel() * 8 + self.batch * 4
+        dev = c["A0"].buf.device
+        ns, As, Bs = c["ns"], c["As"], c["Bs"]
+        h = len(ns) // 2
+        c["e2e_halves"] = [self._half(dev, c["lib"], ns[lo:hi], As[lo:hi], Bs[lo:hi])
+                           for lo, hi in ((0, h), (h, len(ns)))]
+        c["copy_stream"] = torch.cuda.Stream(dev)
+        h2d = sum(hc["hA"].numel() * 8 + hc["hB"].numel() * 8 for hc in c["e2e_halves"])
+        d2h = sum(hc["hX"].numel() * 8 + hc["b"] * 4 for hc in c["e2e_halves"])
+        return h2d, d2h
 
     def e2e_step(self, c):
-        c["A"][0].buf.copy_(c["hA"], non_blocking=True)
-        c["B"][0].buf.copy_(c["hB"], non_blocking=True)
-        c["graphs"][0].replay()
-        c["hX"].copy_(c["B"][0].buf, non_blocking=True)
-        c["hInfo"].copy_(c["info"], non_blocking=True)
+        import torch
+        main, cs = torch.cuda.current_stream(), c["copy_stream"]
+        cs.wait_stream(main)                      # the previous step is done with the buffers
+        arrived = []
+        with torch.cuda.stream(cs):
+            for hc in c["e2e_halves"]:
+                hc["A"].buf.copy_(hc["hA"], non_blocking=True)
+                hc["B"].buf.copy_(hc["hB"], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                arrived.append(ev)
+        for hc, ev in zip(c["e2e_halves"], arrived):
+            main.wait_event(ev)
+            hc["graph"].replay()
+            done = torch.cuda.Event()
+            done.record(main)
+            with torch.cuda.stream(cs):
+                cs.wait_event(done)
+                hc["hX"].copy_(hc["B"].buf, non_blocking=True)
+                hc["hInfo"].copy_(hc["info"], non_blocking=True)
+        main.wait_stream(cs)                      # the step ends when the results are home
 
     def accuracy(self, c, last):
         import torch
